@@ -1,0 +1,289 @@
+/*
+ * mflo_gpu.h — C ABI of the GB300 (sm_103a) implementation of mesoflow's
+ * per-box explicit right-hand side and SSP-RK3 stage update.
+ *
+ * The boundary is plain C: raw device pointers, strides, sizes and POD
+ * parameter tables.  An AMReX-based mesoflow driver calls these entry points
+ * in place of the bodies of
+ *   mflo::compute_dsdt_flow        Source/mflo_evolve.cpp:543-682
+ *   mflo::update_cutcell_data      Source/mflo_evolve.cpp:495-519
+ *   RK3 stage algebra              Source/mflo_evolve.cpp:276-311
+ *   mflo::compute_dsdt_chemistry   Source/mflo_evolve.cpp:684-720
+ *   mflo::compute_residual_norms   Source/mflo_evolve.cpp:91-112
+ *   mflo::update_primitive_vars    Source/mflo_evolve.cpp:114-171
+ *   mflo::clip_neg_speciesconc     Source/mflo_evolve.cpp:521-540
+ *   mflo::EstTimeStep              Source/mflo_timestep.cpp:53-153
+ *   mflo::FillPatch (single level) Source/mflo_gridwork.cpp:135-146 + Source/mflo_bcfill.H
+ * keeping the reference's state layout (Source/globalDefines.H:5-32):
+ * component-major AMReX Array4<Real> boxes, FP64.
+ *
+ * Memory: the caller owns every state array.  The library owns only its
+ * scratch (face-flux and reconstruction buffers, box tables, graphs), which it
+ * allocates on first use and frees in mfg_finalize().
+ *
+ * Errors: every entry point returns an int status (MFG_OK on success).  Faults
+ * detected on the device (NaN in dsdt, negative pressure, bad box, bounded
+ * wait timeout) become sticky bits read by mfg_status(); kernels never trap.
+ *
+ * Threading: entry points are asynchronous on the caller's stream (passed as
+ * void*, a cudaStream_t) except those that return host values, which
+ * synchronize that stream.  mfg_init() is not thread-safe.
+ */
+#ifndef MFLO_GPU_H_
+#define MFLO_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- layout constants (Source/globalDefines.H:5-32) -------------------- */
+#define MFG_RHO_INDX    0
+#define MFG_RHOU_INDX   1
+#define MFG_RHOV_INDX   2
+#define MFG_RHOW_INDX   3
+#define MFG_RHOE_INDX   4
+#define MFG_DENS_INDX   5
+#define MFG_VELX_INDX   6
+#define MFG_VELY_INDX   7
+#define MFG_VELZ_INDX   8
+#define MFG_PRES_INDX   9
+#define MFG_TEMP_INDX   10
+#define MFG_VFRAC_INDX  11
+#define MFG_FLO_NVARS   12
+#define MFG_NCVARS      5
+
+#define MFG_MAX_SPECIES   16
+#define MFG_MAX_REACTIONS 16
+#define MFG_NGROW         3      /* ghost width of Sborder (mflo_evolve.cpp:253) */
+
+/* ---- status codes --------------------------------------------------------- */
+#define MFG_OK                0
+#define MFG_ERR_ARG           1   /* bad argument / box descriptor */
+#define MFG_ERR_NAN           2   /* "NaN detected in dsdt" (div_3d.H:72-75) */
+#define MFG_ERR_NEG_PRESSURE  3   /* "Pressure has gone negative" (mflo_evolve.cpp:162-167) */
+#define MFG_ERR_SCHEME        4   /* "unknown hyperbolics scheme" (compute_flux_3d.H:273-276) */
+#define MFG_ERR_TIMEOUT       5   /* a bounded device wait gave up */
+#define MFG_ERR_CUDA          6   /* a CUDA runtime call failed */
+#define MFG_ERR_STATE         7   /* called before mfg_init / unsupported configuration */
+
+/* sticky device status bits (mfg_status) */
+#define MFG_STATUS_NAN           0x1u
+#define MFG_STATUS_NEG_PRESSURE  0x2u
+#define MFG_STATUS_TIMEOUT       0x4u
+#define MFG_STATUS_BAD_BOX       0x8u
+
+/* ---- thermo / transport / boundary enums ---------------------------------- */
+/* thermo families found in the reference's per-case thermo.H plugins */
+#define MFG_THERMO_MOLAR        0  /* calorically perfect molar mixture:
+                                      models/catalystCylinder/thermo.H:36-156,
+                                      tests/Cartesian/ShockTube_N2/thermo.H:38-132 */
+#define MFG_THERMO_MASS_SINGLE  1  /* single gas, p=(gamma-1) rho e:
+                                      tests/Cartesian/TaylorGreen/thermo.H:36-80,
+                                      models/porousParticle/thermo.H */
+#define MFG_THERMO_BG_GAS       2  /* molar mixture plus untracked background gas:
+                                      py_utils/rxnscheme_writer/example/thermo.H */
+
+/* energy form of get_e_from_rpc for the molar family */
+#define MFG_EFORM_MOLAR_CV  0      /* sum(cv_k c_k) T / rho   (catalystCylinder/thermo.H:131-156) */
+#define MFG_EFORM_MASS_CV   1      /* T * sum(cv_k/W_k x_k)    (ShockTube_N2/thermo.H:110-132) */
+
+#define MFG_TRANSPORT_CONST        0  /* coefficient = gas value */
+#define MFG_TRANSPORT_VFRAC_BLEND  1  /* gas*vfrac + solid*(1-vfrac) (catalystCylinder/transport.H) */
+
+/* physical boundary kinds, numbered as mflo.lo_bc / mflo.hi_bc (Source/mflo.cpp:86-142) */
+#define MFG_BC_INT_DIR   0  /* periodic */
+#define MFG_BC_FOEXTRAP  2
+#define MFG_BC_EXT_DIR   3
+#define MFG_BC_WALL      6  /* reflect_even, reflect_odd for momenta/velocities */
+
+/* ext_dir ghost-state templates (the per-case externalbc functor, externbc.H) */
+#define MFG_EXT_FIXED_STATE      0  /* s_ext = given state; optionally PRES from the interior
+                                       (tests/Cartesian/ShockTube_N2/externbc.H) */
+#define MFG_EXT_PRESSURE_INLET   1  /* dens,pres,species fixed; normal velocity = |u_int|
+                                       (models/porousParticle/externbc.H:25-43) */
+#define MFG_EXT_PRESSURE_OUTLET  2  /* pres fixed; dens,velocity,species from the interior
+                                       (models/porousParticle/externbc.H:44-58) */
+#define MFG_EXT_VELOCITY_INLET   3  /* dens,velocity,pres,species fixed (conserved from prim) */
+
+/* ---- views ---------------------------------------------------------------- */
+/* Mirror of amrex::Array4<Real>: p[(i-begin0) + (j-begin1)*jstride
+ * + (k-begin2)*kstride + n*nstride]; end is exclusive. */
+typedef struct mfg_array4 {
+    double*  p;
+    int64_t  jstride;
+    int64_t  kstride;
+    int64_t  nstride;
+    int      begin[3];
+    int      end[3];
+    int      ncomp;
+} mfg_array4;
+
+/* One AMReX box of a level (the body of one MFIter iteration). */
+typedef struct mfg_box {
+    int        lo[3];       /* valid cells, inclusive (Box::smallEnd)              */
+    int        hi[3];       /* valid cells, inclusive (Box::bigEnd)                */
+    mfg_array4 sborder;     /* state grown by >= MFG_NGROW ghost cells (Sborder)   */
+    mfg_array4 dsdt;        /* RHS on the valid box; p == NULL: not stored          */
+    mfg_array4 s_old;       /* phi_old on the valid box (RK base state)            */
+    mfg_array4 s_new;       /* phi_new on the valid box (RK stage output)          */
+    mfg_array4 flux[3];     /* face fluxes, nodal in d (for reflux); p == NULL: skip */
+    int        level;       /* index into the geometry array of batched calls      */
+    int        pad_;
+} mfg_box;
+
+typedef struct mfg_geom {
+    double dx[3];
+    double prob_lo[3];
+    int    domain_lo[3];
+    int    domain_hi[3];
+    int    is_periodic[3];
+    int    pad_;
+} mfg_geom;
+
+typedef struct mfg_extbc {
+    int    kind;                  /* MFG_EXT_* */
+    int    keep_interior_pres;    /* FIXED_STATE: PRES_INDX copied from the boundary cell */
+    double dens, pres;
+    double vel[3];
+    double spec[MFG_MAX_SPECIES];
+    double state[MFG_FLO_NVARS + MFG_MAX_SPECIES];   /* FIXED_STATE ghost state */
+} mfg_extbc;
+
+/* The per-case plugin headers and mflo.* runtime parameters, as tables. */
+typedef struct mfg_params {
+    /* species + thermo (species.H, species.cpp, thermo.H) */
+    int    nspec;                              /* NUM_SPECIES (1..MFG_MAX_SPECIES) */
+    int    ngas;                               /* NUM_GAS_SPECIES: species [0,ngas) are gas */
+    int    thermo_kind;                        /* MFG_THERMO_* */
+    int    energy_form;                        /* MFG_EFORM_* (molar family) */
+    double R_univ;                             /* gas constant of the molar / bg families */
+    double gas_R;                              /* specific gas constant (mass-single family) */
+    double gamma_single;                       /* gamma (mass-single family) */
+    double bg_molwt;                           /* BG_GAS_MWT (bg family) */
+    double molwt[MFG_MAX_SPECIES];
+    double gamma[MFG_MAX_SPECIES + 1];         /* gas species; [ngas] = background gas */
+    double advect_flag[MFG_MAX_SPECIES];
+    /* transport (transport.H compute_spec_dcoeff, userfuncs.H compute_fluid_transport) */
+    int    visc_mode, cond_mode;               /* MFG_TRANSPORT_* */
+    double visc_gas, visc_solid;
+    double cond_gas, cond_solid;
+    int    diff_mode[MFG_MAX_SPECIES];
+    double diff_gas[MFG_MAX_SPECIES];
+    double diff_solid[MFG_MAX_SPECIES];
+    /* numerics (Source/mflo.H:227-259) */
+    int    order_hyp;                          /* 1, 2, 4 or 5 */
+    int    do_ns;                              /* mflo.solve_navier_stokes */
+    int    species_in_solid;
+    int    conj_ht;                            /* mflo.conjugate_heat_transfer */
+    double dissfactor;
+    double solid_temp;                         /* get_solid_t_from_rhoe */
+    double cfl;
+    /* chemistry (chemistry.H compute_spec_source) */
+    int    chem_on;
+    int    nreact;
+    double nu[MFG_MAX_REACTIONS][MFG_MAX_SPECIES];    /* net stoichiometry (rxnarray) */
+    double order[MFG_MAX_REACTIONS][MFG_MAX_SPECIES]; /* concentration exponents (|rxnarray| of reactants) */
+    double A[MFG_MAX_REACTIONS];               /* rateconsts, or Arrhenius pre-exponential */
+    double Ea[MFG_MAX_REACTIONS];              /* activation energy J/mol; 0 = table form */
+    /* boundaries (mflo.lo_bc / mflo.hi_bc, externbc.H) */
+    int    bc_lo[3], bc_hi[3];                 /* MFG_BC_* */
+    mfg_extbc ext_lo[3], ext_hi[3];
+} mfg_params;
+
+/* ---- library lifetime ----------------------------------------------------- */
+
+/* Validates the parameter tables and uploads them to device constant memory.
+ * Replaces the compile-time plugin includes (thermo.H, transport.H,
+ * chemistry.H, species.cpp) and mflo::ReadParameters (Source/mflo.cpp:263-307). */
+int mfg_init(const mfg_params* params);
+
+/* Frees the library's scratch (face fluxes, box tables, graphs). */
+int mfg_finalize(void);
+
+/* Reads (and optionally clears) the sticky device status bits.  Synchronizes. */
+int mfg_status(uint32_t* flags, int clear);
+
+/* Library version string. */
+const char* mfg_version(void);
+
+/* ---- per-level operations on a box list (all boxes share geom) ------------ */
+
+/* Single-level ghost fill of every box's sborder from the level's valid data
+ * (s_src selects which array of each box holds the valid data: 0 = s_old,
+ * 1 = s_new) plus the physical boundary conditions.
+ * Replaces FillPatch(lev, time, Sborder, 0, ncomp) at level 0
+ * (Source/mflo_gridwork.cpp:135-146, Source/mflo_bcfill.H:13-129). */
+int mfg_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                   int s_src, double time, void* stream);
+
+/* Immersed-boundary cut-cell ghost treatment, in place on sborder (valid cells).
+ * Replaces mflo::update_cutcell_data (Source/mflo_evolve.cpp:495-519)
+ * -> update_cutcells (Source/Src_3d/ib_utils.H:272-436). */
+int mfg_cutcells(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                 double time, void* stream);
+
+/* Flow RHS dsdt from sborder (and face fluxes when flux[d].p != NULL).
+ * Replaces mflo::compute_dsdt_flow (Source/mflo_evolve.cpp:543-682):
+ * compute_flux (compute_flux_3d.H:88-430) + update_residual (div_3d.H:13-76). */
+int mfg_compute_dsdt_flow(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                          double time, double dt, void* stream);
+
+/* Fused RHS + RK3 stage algebra (stage = 1, 2 or 3), writing s_new:
+ *   1: s_new = sborder + dt*L(sborder)                       (mflo_evolve.cpp:283)
+ *   2: s_new = ((s_new + dt*L(sborder)) + 3*s_old) * 1/4     (mflo_evolve.cpp:296-298)
+ *   3: s_new = (s_old + 2*(s_new + dt*L(sborder))) * third   (mflo_evolve.cpp:309-311)
+ * dsdt is also stored when dsdt.p != NULL. */
+int mfg_rk3_stage(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                  int stage, double time, double dt, void* stream);
+
+/* Species reaction source added to dsdt on the valid box (s_new holds the
+ * state).  Replaces compute_dsdt_chemistry (Source/mflo_evolve.cpp:684-720). */
+int mfg_chem_source(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                    double time, void* stream);
+
+/* Strang chemistry sub-step over dt: s_old = state after the flow stages,
+ * s_new = result; explicit SSP-RK3 of the reaction source, as the AMReX
+ * TimeIntegrator default (Source/mflo_evolve.cpp:470-493, Source/mflo.cpp:300-305). */
+int mfg_chem_substep(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                     double time, double dt, void* stream);
+
+/* cons -> prim refresh of s_new plus the negative-pressure check
+ * (Source/mflo_evolve.cpp:114-171); returns MFG_ERR_NEG_PRESSURE. Synchronizes. */
+int mfg_update_primitive_vars(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                              void* stream);
+
+/* Negative species concentrations of s_new set to 0 (Source/mflo_evolve.cpp:521-540). */
+int mfg_clip_species(const mfg_box* boxes, int nbox, void* stream);
+
+/* L2 norms of (s_new - s_old)/dt (components < VFRAC scaled by s_old VFRAC) per
+ * component into out[ncomp] (host).  Source/mflo_evolve.cpp:91-112. Synchronizes. */
+int mfg_residual_norms(const mfg_box* boxes, int nbox, double dt,
+                       double* out, void* stream);
+
+/* CFL / diffusion time-step estimate of s_new, cfl applied
+ * (Source/mflo_timestep.cpp:53-153).  *dt_out on the host.  Synchronizes. */
+int mfg_est_timestep(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                     double time, double* dt_out, void* stream);
+
+/* One coarse step of a single level (Source/mflo_evolve.cpp:251-318 with the
+ * bookends of mflo::EvolveAMR :33-58): phi_old <- phi_new; three RK3 stages of
+ * fill patch, cut cells and the fused RHS + stage update; the Strang
+ * chemistry sub-step unless only_flow; primitive refresh (negative pressure
+ * -> MFG_ERR_NEG_PRESSURE); species clipping when clip != 0; residual norms
+ * into resnorms[ncomp] when non-NULL.  Returns MFG_ERR_NAN when the "NaN
+ * detected in dsdt" condition occurred.  Synchronizes the stream. */
+int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                      double time, double dt, int only_flow, int clip,
+                      double* resnorms, void* stream);
+
+/* Selects the WENO5 nonlinear-weight normalisation: fast != 0 uses one
+ * division per reconstructed value (default), 0 follows the reference's
+ * four reciprocals (flux_schemes.H:407-414) operation for operation. */
+int mfg_set_weno_mode(int fast);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFLO_GPU_H_ */

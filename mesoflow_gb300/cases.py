@@ -1,0 +1,373 @@
+"""Case set-ups: parameter tables (the reference's per-case plugin headers and
+inputs files as mfg_params) and seeded synthetic initial states.
+
+Cases
+  sod               tests/Cartesian/ShockTube_N2 (single species N2, R_univ = 1)
+  taylor_green_mix  3D Taylor-Green vortex (tests/Cartesian/TaylorGreen/Prob.H
+                    velocity field) in a 5-species calorically perfect mixture
+  porous_ib         pressure-driven flow through a seeded sphere pack, immersed
+                    boundary (models/porousParticle pattern)
+  catalyst          catalyst block with surface reactions (models/stagFlowCatalyst /
+                    rxnscheme example pattern)
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import abi
+from .level import chop, geometry
+
+RU = 8.31446261815324
+
+
+def _base_params(nspec):
+    p = abi.Params()
+    C.memset(C.byref(p), 0, C.sizeof(p))
+    p.nspec = nspec
+    p.ngas = nspec
+    p.R_univ = RU
+    p.order_hyp = 2           # Source/mflo.H:241
+    p.dissfactor = 0.5
+    p.do_ns = 1
+    p.species_in_solid = 1
+    p.solid_temp = 300.0
+    p.cfl = 0.7
+    for s in range(nspec):
+        p.advect_flag[s] = 1.0
+    for d in range(3):
+        p.bc_lo[d] = abi.BC_FOEXTRAP
+        p.bc_hi[d] = abi.BC_FOEXTRAP
+    return p
+
+
+# ---------------------------------------------------------------------------
+# host thermodynamics for building initial states (numpy, vectorised)
+# ---------------------------------------------------------------------------
+def temperature(P_, rho, pres, spec):
+    """get_t_from_rpc of the case's thermo family."""
+    if P_.thermo_kind == abi.THERMO_MASS_SINGLE:
+        return pres / P_.gas_R / rho
+    if P_.thermo_kind == abi.THERMO_BG_GAS:
+        sum_ci = sum(spec[s] for s in range(P_.ngas))
+        sum_cm = sum(spec[s] * P_.molwt[s] for s in range(P_.ngas))
+        return pres / ((sum_ci + (rho - sum_cm) / P_.bg_molwt) * RU)
+    sum_ci = sum(spec[s] for s in range(P_.ngas))
+    return pres / (sum_ci * P_.R_univ)
+
+
+def energy(P_, rho, pres, spec):
+    """get_e_from_rpc of the case's thermo family (specific internal energy)."""
+    if P_.thermo_kind == abi.THERMO_MASS_SINGLE:
+        return pres / (P_.gamma_single - 1.0) / rho
+    T = temperature(P_, rho, pres, spec)
+    if P_.thermo_kind == abi.THERMO_BG_GAS:
+        sum_cm = sum(spec[s] * P_.molwt[s] for s in range(P_.ngas))
+        cbg = (rho - sum_cm) / P_.bg_molwt
+        scv = sum(RU / (P_.gamma[s] - 1.0) * spec[s] for s in range(P_.ngas))
+        scv = scv + RU / (P_.gamma[P_.ngas] - 1.0) * cbg
+        return scv * T / rho
+    if P_.energy_form == abi.EFORM_MASS_CV:
+        sum_ci = sum(spec[s] for s in range(P_.ngas))
+        cvbar = sum(P_.R_univ / (P_.gamma[s] - 1.0) / P_.molwt[s] * (spec[s] / sum_ci) for s in range(P_.ngas))
+        return cvbar * T
+    scv = sum(P_.R_univ / (P_.gamma[s] - 1.0) * spec[s] for s in range(P_.ngas))
+    return scv * T / rho
+
+
+def state_from_prim(P_, rho, u, v, w, pres, spec, vfrac):
+    """Full state (ncomp, Z, Y, X) from primitive fields (as the cases' initdata)."""
+    ns = P_.nspec
+    shp = np.shape(rho)
+    S = np.zeros((abi.FLO_NVARS + ns,) + shp)
+    S[abi.DENS], S[abi.VELX], S[abi.VELY], S[abi.VELZ], S[abi.PRES] = rho, u, v, w, pres
+    S[abi.VFRAC] = vfrac
+    for s in range(ns):
+        S[abi.FLO_NVARS + s] = spec[s]
+    S[abi.TEMP] = temperature(P_, rho, pres, spec)
+    S[abi.RHO] = rho
+    S[abi.RHOU], S[abi.RHOV], S[abi.RHOW] = rho * u, rho * v, rho * w
+    S[abi.RHOE] = rho * energy(P_, rho, pres, spec) + 0.5 * rho * (u * u + v * v + w * w)
+    return S
+
+
+class Case:
+    """Parameters, geometry, box layout and initial state of one configuration."""
+
+    def __init__(self, name, params, n_cell, prob_lo, prob_hi, periodic, max_grid, state, meta=None):
+        self.name = name
+        self.params = params
+        self.n_cell = tuple(n_cell)
+        self.domain_lo = (0, 0, 0)
+        self.domain_hi = tuple(n - 1 for n in n_cell)
+        self.geom = geometry(self.domain_lo, self.domain_hi, prob_lo, prob_hi, periodic)
+        self.boxes = chop(self.domain_lo, self.domain_hi, max_grid)
+        self.state = state
+        self.meta = meta or {}
+
+    @property
+    def ncomp(self):
+        return abi.FLO_NVARS + self.params.nspec
+
+    @property
+    def shape_zyx(self):
+        return (self.n_cell[2], self.n_cell[1], self.n_cell[0])
+
+
+def _centers(n_cell, prob_lo, prob_hi):
+    ax = []
+    for d in range(3):
+        dx = (prob_hi[d] - prob_lo[d]) / n_cell[d]
+        ax.append(prob_lo[d] + (np.arange(n_cell[d]) + 0.5) * dx)
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    return X, Y, Z
+
+
+# ---------------------------------------------------------------------------
+def sod(n_cell=(256, 4, 4), order=5, max_grid=64, axis=0):
+    """Sod shock tube along `axis` (tests/Cartesian/ShockTube_N2: N2, gamma 1.4,
+    R_univ = 1 because inputs_x sets prob.R_univ while userfuncs.cpp reads
+    prob.univr).  Left rho=1, p=1; right rho=0.125, p=0.1.  Outflow (foextrap)
+    along the tube, periodic across."""
+    P = _base_params(1)
+    P.thermo_kind = abi.THERMO_MOLAR
+    P.energy_form = abi.EFORM_MASS_CV
+    P.R_univ = 1.0
+    P.molwt[0] = 0.028
+    P.gamma[0] = 1.4
+    P.order_hyp = order
+    P.cfl = 0.5
+    for d in range(3):
+        P.bc_lo[d] = abi.BC_FOEXTRAP if d == axis else abi.BC_INT_DIR
+        P.bc_hi[d] = abi.BC_FOEXTRAP if d == axis else abi.BC_INT_DIR
+    n_cell = list(n_cell)
+    if axis != 0:
+        n_cell[0], n_cell[axis] = n_cell[axis], n_cell[0]
+    prob_hi = [0.125, 0.125, 0.125]
+    prob_hi[axis] = 1.0
+    X, Y, Z = _centers(n_cell, (0, 0, 0), prob_hi)
+    xa = (X, Y, Z)[axis]
+    left = xa < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    pres = np.where(left, 1.0, 0.1)
+    spec = [rho / 0.028]
+    zero = np.zeros_like(rho)
+    S = state_from_prim(P, rho, zero, zero, zero, pres, spec, np.ones_like(rho))
+    periodic = [d != axis for d in range(3)]
+    return Case("sod", P, n_cell, (0, 0, 0), prob_hi, periodic, max_grid, S, {"axis": axis})
+
+
+def taylor_green_mix(n=256, order=5, max_grid=64, seed=20261203, v0=10.0):
+    """3D Taylor-Green vortex on [-1,1]^3 (velocity of tests/Cartesian/TaylorGreen/
+    Prob.H) plus 1% Gaussian noise, in a 5-species calorically perfect molar
+    mixture at p = 1e5 Pa, T = 300 K with mass fractions ~ Dirichlet(2) per cell.
+    mu = rho0 v0 L / Re (Re = 1600, TaylorGreen/userfuncs.H), k = mu cp / Pr,
+    D_k = 1e-5.  Periodic."""
+    ns = 5
+    P = _base_params(ns)
+    P.thermo_kind = abi.THERMO_MOLAR
+    P.energy_form = abi.EFORM_MOLAR_CV
+    W = [0.028, 0.032, 0.044, 0.018, 0.040]
+    G = [1.4, 1.4, 1.3, 1.33, 1.67]
+    for s in range(ns):
+        P.molwt[s], P.gamma[s] = W[s], G[s]
+        P.diff_gas[s] = 1e-5
+    mu = 1.0 * v0 * 1.0 / 1600.0
+    P.visc_gas = mu
+    P.cond_gas = mu * 1000.0 / 0.7
+    P.order_hyp = order
+    P.cfl = 0.4
+    for d in range(3):
+        P.bc_lo[d] = P.bc_hi[d] = abi.BC_INT_DIR
+    rng = np.random.default_rng(seed)
+    shape = (n, n, n)
+    X, Y, Z = _centers((n, n, n), (-1, -1, -1), (1, 1, 1))
+    pi = math.pi
+    u = v0 * np.sin(pi * X) * np.cos(pi * Y) * np.cos(pi * Z)
+    v = -v0 * np.cos(pi * X) * np.sin(pi * Y) * np.cos(pi * Z)
+    w = np.zeros(shape)
+    u = u + 0.01 * v0 * rng.standard_normal(shape)
+    v = v + 0.01 * v0 * rng.standard_normal(shape)
+    w = w + 0.01 * v0 * rng.standard_normal(shape)
+    Yk = rng.dirichlet([2.0] * ns, size=shape)  # (Z,Y,X,ns)
+    Yk = np.moveaxis(Yk, -1, 0)
+    pres = np.full(shape, 1e5)
+    T = 300.0
+    sum_y_w = sum(Yk[s] / W[s] for s in range(ns))
+    rho = pres / (RU * T * sum_y_w)
+    spec = [rho * Yk[s] / W[s] for s in range(ns)]
+    S = state_from_prim(P, rho, u, v, w, pres, spec, np.ones(shape))
+    return Case("taylor_green_mix", P, (n, n, n), (-1, -1, -1), (1, 1, 1), (1, 1, 1), max_grid, S)
+
+
+def sphere_pack_vfrac(n, seed, solid_frac, rmin=4.0, rmax=12.0, smooth=True):
+    """Fluid volume fraction of a seeded random pack of overlapping spheres
+    (radii uniform in [rmin, rmax] cells) grown until the solid fraction reaches
+    solid_frac; 8-corner sampling as the reference's initdata
+    (tests/ImmBoundary/subsonicCylinder/Prob.H:39-59), then a 2-cell box filter
+    and snapping of near-0/1 values so that pure cells stay exactly 0 or 1."""
+    rng = np.random.default_rng(seed)
+    nn = n + 1
+    ax = np.arange(nn, dtype=np.float64)
+    solid_c = np.zeros((nn, nn, nn), dtype=bool)  # corner (k,j,i) inside a sphere
+    centers = []
+    while True:
+        c = rng.uniform(0, n, size=3)
+        r = rng.uniform(rmin, rmax)
+        centers.append((c, r))
+        lo = np.maximum(np.floor(c - r).astype(int), 0)
+        hi = np.minimum(np.ceil(c + r).astype(int) + 1, nn)
+        zz, yy, xx = np.meshgrid(ax[lo[2]:hi[2]], ax[lo[1]:hi[1]], ax[lo[0]:hi[0]], indexing="ij")
+        inside = (xx - c[0]) ** 2 + (yy - c[1]) ** 2 + (zz - c[2]) ** 2 <= r * r
+        solid_c[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] |= inside
+        fluid = (~solid_c).astype(np.float64)
+        vf = 0.125 * sum(fluid[kk:kk + n, jj:jj + n, ii:ii + n] for kk in (0, 1) for jj in (0, 1) for ii in (0, 1))
+        if 1.0 - vf.mean() >= solid_frac:
+            break
+    if smooth:
+        for axis in range(3):  # separable 3-point average, applied twice: ~2-cell box filter
+            for _ in range(2):
+                pad = [(0, 0)] * 3
+                pad[axis] = (1, 1)
+                q = np.pad(vf, pad, mode="edge")
+                sl = [slice(None)] * 3
+                acc = 0.0
+                for o in range(3):
+                    sl[axis] = slice(o, o + n)
+                    acc = acc + q[tuple(sl)]
+                vf = acc / 3.0
+        vf[vf >= 0.999] = 1.0
+        vf[vf <= 0.001] = 0.0
+    return vf
+
+
+def porous_ib(n=256, order=2, max_grid=64, seed=3, solid_frac=0.4, dx=2e-6, p_out=1e5, dp_rel=1e-3):
+    """Pressure-driven flow through a seeded sphere pack (models/porousParticle
+    pattern): air (W = 0.0289, gamma 1.4, p = rho R_air T), mu = 1e-5,
+    k = 0.014, D = 1e-5, species_in_solid = 0; x: pressure inlet
+    p_in = (1 + dp_rel) p_out / pressure outlet p_out (ext_dir), y/z: walls."""
+    P = _base_params(1)
+    P.thermo_kind = abi.THERMO_MASS_SINGLE
+    W = 0.0289
+    P.molwt[0] = W
+    P.gamma[0] = 1.4
+    P.gamma_single = 1.4
+    P.gas_R = RU / W
+    P.visc_gas = 1e-5
+    P.cond_gas = 0.014
+    P.diff_gas[0] = 1e-5
+    P.species_in_solid = 0
+    P.order_hyp = order
+    P.cfl = 0.4
+    T = 300.0
+    p_in = p_out * (1.0 + dp_rel)
+    rho_in = p_in / (P.gas_R * T)
+    P.bc_lo[0] = P.bc_hi[0] = abi.BC_EXT_DIR
+    for d in (1, 2):
+        P.bc_lo[d] = P.bc_hi[d] = abi.BC_WALL
+    P.ext_lo[0].kind = abi.EXT_PRESSURE_INLET
+    P.ext_lo[0].dens = rho_in
+    P.ext_lo[0].pres = p_in
+    P.ext_lo[0].spec[0] = rho_in / W
+    P.ext_hi[0].kind = abi.EXT_PRESSURE_OUTLET
+    P.ext_hi[0].pres = p_out
+    vf = sphere_pack_vfrac(n, seed, solid_frac)
+    shape = (n, n, n)
+    rho = np.full(shape, p_out / (P.gas_R * T))
+    zero = np.zeros(shape)
+    S = state_from_prim(P, rho, zero, zero, zero, np.full(shape, p_out), [rho / W], vf)
+    L = n * dx
+    return Case("porous_ib", P, shape, (0, 0, 0), (L, L, L), (0, 0, 0), max_grid, S,
+                {"p_in": p_in, "p_out": p_out, "mu": 1e-5})
+
+
+def permeability(case, state):
+    """Darcy permeability k = mu <u_x>_superficial L_x / dp (superficial
+    velocity: the volume average of rho u_x / rho over all cells, solid = 0)."""
+    m = case.meta
+    rho = state[abi.RHO]
+    ux = np.where(state[abi.VFRAC] > 0, state[abi.RHOU] / np.where(rho > 0, rho, 1.0), 0.0) * state[abi.VFRAC]
+    Lx = case.n_cell[0] * case.geom.dx[0]
+    return m["mu"] * float(ux.mean()) * Lx / (m["p_in"] - m["p_out"])
+
+
+def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, block=True, u_in=1.0, dx=1e-5,
+             arrhenius=True):
+    """Catalyst block with explicit surface chemistry (models/stagFlowCatalyst /
+    rxnscheme example pattern): 8 gas species + 2 non-advected site species
+    (molar mixture, R = RU); mass-action surface reactions gas_a + site_b ->
+    gas_c + site_d with log10 A ~ U[3, 8] and Ea ~ U[40, 120] kJ/mol (seeded),
+    or the reference's table form (Ea = 0) when arrhenius is False.
+    Diffusivities blend gas/solid with vfrac; species_in_solid = 1.
+    x: velocity inlet u_in / outflow (foextrap); y, z: walls.  The immersed
+    solid is a block in the middle third plus a seeded sphere pack."""
+    ng, nsite = 8, 2
+    ns = ng + nsite
+    P = _base_params(ns)
+    P.thermo_kind = abi.THERMO_MOLAR
+    P.energy_form = abi.EFORM_MOLAR_CV
+    P.ngas = ng
+    rng = np.random.default_rng(seed)
+    W = [0.028, 0.032, 0.044, 0.018, 0.002, 0.016, 0.030, 0.026]
+    G = [1.4, 1.4, 1.3, 1.33, 1.41, 1.31, 1.4, 1.3]
+    for s in range(ng):
+        P.molwt[s], P.gamma[s] = W[s], G[s]
+        P.diff_mode[s] = abi.TRANSPORT_VFRAC_BLEND
+        P.diff_gas[s] = 1e-5 * (1.0 + s / ng)
+        P.diff_solid[s] = 1e-6 * (1.0 + s / ng)
+    for s in range(ng, ns):
+        P.molwt[s] = 0.001
+        P.advect_flag[s] = 0.0
+        P.diff_mode[s] = abi.TRANSPORT_CONST
+        P.diff_gas[s] = 0.0
+    P.visc_gas = 2.15e-5
+    P.cond_gas = 8.25e-2
+    P.species_in_solid = 1
+    P.order_hyp = order
+    P.cfl = 0.4
+    P.chem_on = 1
+    P.nreact = nreact
+    for r in range(nreact):
+        a, c = rng.choice(ng, size=2, replace=False)
+        b = ng + r % nsite
+        d = ng + (r + 1) % nsite
+        P.nu[r][a] = -1.0
+        P.nu[r][b] += -1.0
+        P.nu[r][c] += 1.0
+        P.nu[r][d] += 1.0
+        P.order[r][a] = 1.0
+        P.order[r][b] = 1.0
+        P.A[r] = 10.0 ** rng.uniform(3.0, 8.0)
+        P.Ea[r] = rng.uniform(40e3, 120e3) if arrhenius else 0.0
+    T, pres = 500.0, 1e5
+    x = np.array([0.7, 0.1, 0.05, 0.05, 0.04, 0.03, 0.02, 0.01])
+    ctot = pres / (RU * T)
+    cg = x * ctot
+    rho_in = float(sum(cg[s] * W[s] for s in range(ng)))
+    P.bc_lo[0] = abi.BC_EXT_DIR
+    P.bc_hi[0] = abi.BC_FOEXTRAP
+    for d in (1, 2):
+        P.bc_lo[d] = P.bc_hi[d] = abi.BC_WALL
+    e = P.ext_lo[0]
+    e.kind = abi.EXT_VELOCITY_INLET
+    e.dens = rho_in
+    e.pres = pres
+    e.vel[0] = u_in
+    for s in range(ng):
+        e.spec[s] = cg[s]
+    shape = (n, n, n)
+    vf = sphere_pack_vfrac(n, seed + 1, solid_frac * 0.5, rmin=max(2.0, n / 64), rmax=max(4.0, n / 20))
+    if block:
+        X, Y, Z = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+        inb = (Z >= n // 3) & (Z < 2 * n // 3) & (Y >= n // 4) & (Y < 3 * n // 4) & (X >= n // 4) & (X < 3 * n // 4)
+        vf = np.where(inb.transpose(0, 1, 2), np.minimum(vf, 0.0), vf)  # (z, y, x) indexing == (X, Y, Z) names here
+        vf = np.clip(vf, 0.0, 1.0)
+    spec = [np.full(shape, cg[s]) for s in range(ng)]
+    site = np.where(vf < 1.0, 50.0, 0.0)
+    spec += [site * 0.6, site * 0.4]
+    rho = sum(spec[s] * W[s] for s in range(ng))
+    u = np.where(vf == 1.0, u_in, 0.0)
+    zero = np.zeros(shape)
+    S = state_from_prim(P, rho, u, zero, zero, np.full(shape, pres), spec, vf)
+    L = n * dx
+    return Case("catalyst", P, shape, (0, 0, 0), (L, L, L), (0, 0, 0), max_grid, S, {"u_in": u_in})

@@ -1,0 +1,102 @@
+// Common device-side definitions of the GB300 mesoflow RHS library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "mflo_gpu.h"
+
+namespace mfg {
+
+// State layout (Source/globalDefines.H:5-32)
+constexpr int RHO = 0, RHOU = 1, RHOV = 2, RHOW = 3, RHOE = 4;
+constexpr int DENS = 5, VELX = 6, VELY = 7, VELZ = 8, PRES = 9, TEMP = 10, VFRAC = 11;
+constexpr int NFLO = 12;
+constexpr int NCONS = 5;
+constexpr int MAXS = MFG_MAX_SPECIES;
+constexpr int MAXR = MFG_MAX_REACTIONS;
+
+// Constants with the exact values of Source/mflo_constants.H:4-27.
+constexpr double kTwo3rd = 0.6666666666666666667;
+constexpr double kHalf = 0.5;
+constexpr double kThird = kTwo3rd * kHalf;
+constexpr double kTwelveth = 0.08333333333;  // truncated in the reference
+constexpr double kRU = 8.31446261815324;
+constexpr double kTiny = 1e-20;
+constexpr double kTiny2 = 1e-40;
+
+// Parameters as the kernels read them (derived from mfg_params at mfg_init).
+struct DevParams {
+    int nspec, ngas, thermo_kind, energy_form;
+    double R_univ, gas_R, gamma_single, bg_molwt;
+    double molwt[MAXS];
+    double gamma[MAXS + 1];
+    double cv[MAXS + 1];       // R/(gamma_k - 1) per gas species (+ background gas)
+    double cvmass[MAXS];       // R/(gamma_k - 1)/W_k (mass-cv energy form)
+    double advect_flag[MAXS];
+    int visc_mode, cond_mode;
+    double visc_gas, visc_solid, cond_gas, cond_solid;
+    int diff_mode[MAXS];
+    double diff_gas[MAXS], diff_solid[MAXS];
+    int order_hyp, do_ns, species_in_solid, conj_ht;
+    double dissfactor, solid_temp, cfl;
+    int chem_on, nreact;
+    double nu[MAXR][MAXS];
+    double order[MAXR][MAXS];
+    double A[MAXR], Ea[MAXR];
+    int bc_lo[3], bc_hi[3];
+    mfg_extbc ext_lo[3], ext_hi[3];
+};
+
+// Device view of one box: AMReX Array4 with begin offsets folded into the base.
+struct Fab {
+    double* p;
+    int64_t js, ks, ns;
+    int b0, b1, b2;
+    __host__ __device__ __forceinline__ int64_t off(int i, int j, int k) const {
+        return (int64_t)(i - b0) + (int64_t)(j - b1) * js + (int64_t)(k - b2) * ks;
+    }
+    __host__ __device__ __forceinline__ double& operator()(int i, int j, int k, int n) const {
+        return p[off(i, j, k) + (int64_t)n * ns];
+    }
+};
+
+inline Fab make_fab(const mfg_array4& a) {
+    Fab f;
+    memset(&f, 0, sizeof(f));  // padding included: tables of Fabs are compared bytewise
+    f.p = a.p;
+    f.js = a.jstride;
+    f.ks = a.kstride;
+    f.ns = a.nstride;
+    f.b0 = a.begin[0];
+    f.b1 = a.begin[1];
+    f.b2 = a.begin[2];
+    return f;
+}
+
+// Dense scratch FAB over an index box [lo, lo+len) with ncomp components.
+__host__ __device__ __forceinline__ Fab dense_fab(double* p, const int lo[3], const int len[3]) {
+    Fab f;
+    f.p = p;
+    f.js = len[0];
+    f.ks = (int64_t)len[0] * len[1];
+    f.ns = (int64_t)len[0] * len[1] * len[2];
+    f.b0 = lo[0];
+    f.b1 = lo[1];
+    f.b2 = lo[2];
+    return f;
+}
+
+// Sticky status word in device memory (mfg_status).
+extern __device__ unsigned int g_status;
+
+__device__ __forceinline__ void raise_status(unsigned bits) { atomicOr(&g_status, bits); }
+
+// Rounding-faithful helpers: the intrinsics are never contracted into FMA,
+// so expressions written with them round exactly as the reference's
+// separate multiply and add.
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+}  // namespace mfg

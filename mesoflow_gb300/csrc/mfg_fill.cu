@@ -1,0 +1,327 @@
+// Single-level ghost fill of every box's Sborder (FillPatchSingleLevel with
+// the case's physical boundary functor): copy of valid data from the owning
+// box (periodic images included), then the physical boundaries in the order
+// faces -> edges -> corners.  A cell outside the domain in the set D of
+// non-periodic directions takes its value from the cell one step inward
+// along d*: the highest direction of D whose boundary is ext_dir (the user
+// functor runs after the extrapolation rules and checks x, y, z in turn,
+// Source/mflo_bcfill.H:236-320), otherwise the highest direction of D.
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "mfg_internal.h"
+#include "mfg_physics.cuh"
+
+namespace mfg {
+namespace {
+
+constexpr int TPB = 256;
+
+struct FillBox {
+    int lo[3], hi[3];
+    Fab sb, src;
+};
+
+struct FillGeom {
+    int dlo[3], dhi[3], per[3];
+    int gran;       // owner-map granularity (cells)
+    int mlen[3];    // owner-map extent
+    double dx[3], plo[3];
+};
+
+__device__ __forceinline__ void grown_cell(const FillBox& b, int64_t t, int& i, int& j, int& k, int64_t& n) {
+    const int l0 = b.hi[0] - b.lo[0] + 1 + 2 * MFG_NGROW, l1 = b.hi[1] - b.lo[1] + 1 + 2 * MFG_NGROW,
+              l2 = b.hi[2] - b.lo[2] + 1 + 2 * MFG_NGROW;
+    n = (int64_t)l0 * l1 * l2;
+    int64_t a = t / l0;
+    i = b.lo[0] - MFG_NGROW + (int)(t - a * l0);
+    int64_t kk = a / l1;
+    k = b.lo[2] - MFG_NGROW + (int)kk;
+    j = b.lo[1] - MFG_NGROW + (int)(a - kk * l1);
+}
+
+__global__ void copy_kernel(const FillBox* __restrict__ boxes, FillGeom G, const int* __restrict__ owner, int ncomp) {
+    const FillBox& b = boxes[blockIdx.y];
+    int i, j, k;
+    int64_t n;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    grown_cell(b, t, i, j, k, n);
+    if (t >= n) return;
+    int w[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int len = G.dhi[d] - G.dlo[d] + 1;
+        if (G.per[d]) {
+            while (w[d] < G.dlo[d]) w[d] += len;
+            while (w[d] > G.dhi[d]) w[d] -= len;
+        } else if (w[d] < G.dlo[d] || w[d] > G.dhi[d]) {
+            return;  // physical boundary cell
+        }
+    }
+    const int m0 = (w[0] - G.dlo[0]) / G.gran, m1 = (w[1] - G.dlo[1]) / G.gran, m2 = (w[2] - G.dlo[2]) / G.gran;
+    const int ob = owner[m0 + G.mlen[0] * (m1 + G.mlen[1] * m2)];
+    if (ob < 0) return;  // not covered at this level
+    const FillBox& o = boxes[ob];
+    const int64_t qs = o.src.off(w[0], w[1], w[2]);
+    const int64_t qd = b.sb.off(i, j, k);
+    for (int c = 0; c < ncomp; ++c) b.sb.p[qd + c * b.sb.ns] = o.src.p[qs + c * o.src.ns];
+}
+
+__device__ __forceinline__ bool odd_at_wall(int n) {  // Source/mflo.cpp:98-110
+    return (n >= RHOU && n <= RHOW) || (n >= VELX && n <= VELZ);
+}
+
+// ext_dir ghost state (the case's externalbc functor as a parameterised template)
+template <int NS>
+__device__ void external_state(const mfg_extbc& E, int idir, const double* s_int, double* s_ext, int nc) {
+    const int ns = c_P.nspec;
+    for (int n = 0; n < nc; ++n) s_ext[n] = 0.0;
+    if (E.kind == MFG_EXT_FIXED_STATE) {
+        for (int n = 0; n < nc; ++n) s_ext[n] = E.state[n];
+        if (E.keep_interior_pres) s_ext[PRES] = s_int[PRES];
+        return;
+    }
+    double spec[NS];
+    double dens, pres, vel[3];
+    if (E.kind == MFG_EXT_PRESSURE_INLET) {
+        dens = E.dens;
+        pres = E.pres;
+        const double vm = sqrt((s_int[VELX] * s_int[VELX] + s_int[VELY] * s_int[VELY]) + s_int[VELZ] * s_int[VELZ]);
+        vel[0] = vel[1] = vel[2] = 0.0;
+        vel[idir] = vm;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? E.spec[s] : 0.0;
+    } else if (E.kind == MFG_EXT_PRESSURE_OUTLET) {
+        dens = s_int[DENS];
+        pres = E.pres;
+        vel[0] = s_int[VELX];
+        vel[1] = s_int[VELY];
+        vel[2] = s_int[VELZ];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? s_int[NFLO + s] : 0.0;
+    } else {
+        dens = E.dens;
+        pres = E.pres;
+        vel[0] = E.vel[0];
+        vel[1] = E.vel[1];
+        vel[2] = E.vel[2];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? E.spec[s] : 0.0;
+    }
+    s_ext[DENS] = dens;
+    s_ext[PRES] = pres;
+    s_ext[VELX] = vel[0];
+    s_ext[VELY] = vel[1];
+    s_ext[VELZ] = vel[2];
+    s_ext[TEMP] = thermo_t<NS>(dens, pres, spec);
+    s_ext[RHO] = dens;
+    s_ext[RHOU] = mul(dens, vel[0]);
+    s_ext[RHOV] = mul(dens, vel[1]);
+    s_ext[RHOW] = mul(dens, vel[2]);
+    const double ke = add(add(mul(vel[0], vel[0]), mul(vel[1], vel[1])), mul(vel[2], vel[2]));
+    s_ext[RHOE] = add(mul(dens, thermo_e<NS>(dens, pres, spec)), mul(mul(0.5, dens), ke));
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < ns) s_ext[NFLO + s] = spec[s];
+    s_ext[VFRAC] = s_int[VFRAC];
+}
+
+template <int NS>
+__global__ void bc_kernel(const FillBox* __restrict__ boxes, FillGeom G, int stage, int ncomp) {
+    const FillBox& b = boxes[blockIdx.y];
+    int i, j, k;
+    int64_t n;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    grown_cell(b, t, i, j, k, n);
+    if (t >= n) return;
+    const int iv[3] = {i, j, k};
+    bool out[3];
+    int nout = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        out[d] = !G.per[d] && (iv[d] < G.dlo[d] || iv[d] > G.dhi[d]);
+        nout += out[d];
+    }
+    if (nout != stage) return;
+    const DevParams& P = c_P;
+    int dext = -1, dlast = -1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (!out[d]) continue;
+        dlast = d;
+        const int kind = (iv[d] < G.dlo[d]) ? P.bc_lo[d] : P.bc_hi[d];
+        if (kind == MFG_BC_EXT_DIR) dext = d;
+    }
+    const int ds = (dext >= 0) ? dext : dlast;
+    const bool lo = iv[ds] < G.dlo[ds];
+    const int kind = lo ? P.bc_lo[ds] : P.bc_hi[ds];
+    int sv[3] = {i, j, k};
+    const Fab& S = b.sb;
+    const int64_t qd = S.off(i, j, k);
+    if (dext >= 0) {
+        sv[ds] = lo ? G.dlo[ds] : G.dhi[ds];
+        const int64_t qs = S.off(sv[0], sv[1], sv[2]);
+        double s_int[NFLO + MAXS], s_ext[NFLO + MAXS];
+        for (int c = 0; c < ncomp; ++c) s_int[c] = S.p[qs + c * S.ns];
+        external_state<NS>(lo ? P.ext_lo[ds] : P.ext_hi[ds], ds, s_int, s_ext, ncomp);
+        for (int c = 0; c < ncomp; ++c) S.p[qd + c * S.ns] = s_ext[c];
+    } else if (kind == MFG_BC_FOEXTRAP) {
+        sv[ds] = lo ? G.dlo[ds] : G.dhi[ds];
+        const int64_t qs = S.off(sv[0], sv[1], sv[2]);
+        for (int c = 0; c < ncomp; ++c) S.p[qd + c * S.ns] = S.p[qs + c * S.ns];
+    } else {  // wall: reflect_even, reflect_odd for momenta and velocities
+        sv[ds] = lo ? (2 * G.dlo[ds] - iv[ds] - 1) : (2 * G.dhi[ds] - iv[ds] + 1);
+        const int64_t qs = S.off(sv[0], sv[1], sv[2]);
+        for (int c = 0; c < ncomp; ++c) {
+            const double x = S.p[qs + c * S.ns];
+            S.p[qd + c * S.ns] = odd_at_wall(c) ? -x : x;
+        }
+    }
+}
+
+// Owner map cache (host-built, device-resident); rebuilt when the box layout changes.
+struct OwnerCache {
+    std::vector<int> key;
+    int* d_owner = nullptr;
+    size_t cap = 0;
+    int gran = 1, mlen[3] = {0, 0, 0};
+    FillBox* d_boxes = nullptr;
+    size_t bcap = 0;
+    std::vector<char> table;
+} g_fill;
+
+int igcd(int a, int b) {
+    a = a < 0 ? -a : a;
+    b = b < 0 ? -b : b;
+    while (b) {
+        int t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+cudaError_t ensure_owner(const mfg_box* boxes, int nbox, const mfg_geom& g) {
+    std::vector<int> key;
+    key.reserve(nbox * 6 + 6);
+    for (int d = 0; d < 3; ++d) {
+        key.push_back(g.domain_lo[d]);
+        key.push_back(g.domain_hi[d]);
+    }
+    for (int b = 0; b < nbox; ++b)
+        for (int d = 0; d < 3; ++d) {
+            key.push_back(boxes[b].lo[d]);
+            key.push_back(boxes[b].hi[d]);
+        }
+    if (key == g_fill.key && g_fill.d_owner) return cudaSuccess;
+    int gr = 0;
+    for (int d = 0; d < 3; ++d) gr = igcd(gr, g.domain_hi[d] - g.domain_lo[d] + 1);
+    for (int b = 0; b < nbox; ++b)
+        for (int d = 0; d < 3; ++d) {
+            gr = igcd(gr, boxes[b].lo[d] - g.domain_lo[d]);
+            gr = igcd(gr, boxes[b].hi[d] + 1 - g.domain_lo[d]);
+        }
+    if (gr <= 0) gr = 1;
+    int ml[3];
+    for (int d = 0; d < 3; ++d) ml[d] = (g.domain_hi[d] - g.domain_lo[d] + 1) / gr;
+    std::vector<int> own((size_t)ml[0] * ml[1] * ml[2], -1);
+    for (int b = 0; b < nbox; ++b) {
+        int a[3], e[3];
+        for (int d = 0; d < 3; ++d) {
+            a[d] = (boxes[b].lo[d] - g.domain_lo[d]) / gr;
+            e[d] = (boxes[b].hi[d] + 1 - g.domain_lo[d]) / gr;
+        }
+        for (int z = a[2]; z < e[2]; ++z)
+            for (int y = a[1]; y < e[1]; ++y)
+                for (int x = a[0]; x < e[0]; ++x)
+                    if (x >= 0 && y >= 0 && z >= 0 && x < ml[0] && y < ml[1] && z < ml[2])
+                        own[x + (size_t)ml[0] * (y + (size_t)ml[1] * z)] = b;
+    }
+    cudaError_t e;
+    if (own.size() > g_fill.cap) {
+        if (g_fill.d_owner) cudaFree(g_fill.d_owner);
+        g_fill.d_owner = nullptr;
+        if ((e = cudaMalloc(&g_fill.d_owner, own.size() * sizeof(int))) != cudaSuccess) return e;
+        g_fill.cap = own.size();
+    }
+    if ((e = cudaMemcpy(g_fill.d_owner, own.data(), own.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
+    g_fill.gran = gr;
+    for (int d = 0; d < 3; ++d) g_fill.mlen[d] = ml[d];
+    g_fill.key = key;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+void fill_release() {
+    if (g_fill.d_owner) cudaFree(g_fill.d_owner);
+    if (g_fill.d_boxes) cudaFree(g_fill.d_boxes);
+    g_fill = OwnerCache();
+}
+
+cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g, int s_src, double time,
+                              cudaStream_t st) {
+    (void)time;
+    cudaError_t e = ensure_owner(boxes, nbox, g);
+    if (e != cudaSuccess) return e;
+    // Box tables for both source arrays; re-uploaded only when a descriptor changes.
+    std::vector<FillBox> fb(2 * (size_t)nbox);
+    int64_t maxn = 0;
+    for (int b = 0; b < nbox; ++b) {
+        for (int h = 0; h < 2; ++h) {
+            FillBox& x = fb[(size_t)h * nbox + b];
+            for (int d = 0; d < 3; ++d) {
+                x.lo[d] = boxes[b].lo[d];
+                x.hi[d] = boxes[b].hi[d];
+            }
+            x.sb = make_fab(boxes[b].sborder);
+            x.src = make_fab(h ? boxes[b].s_new : boxes[b].s_old);
+        }
+        int64_t n = 1;
+        for (int d = 0; d < 3; ++d) n *= (boxes[b].hi[d] - boxes[b].lo[d] + 1 + 2 * MFG_NGROW);
+        maxn = n > maxn ? n : maxn;
+    }
+    const size_t bytes = fb.size() * sizeof(FillBox);
+    if (bytes != g_fill.table.size() || std::memcmp(fb.data(), g_fill.table.data(), bytes) != 0) {
+        if (fb.size() > g_fill.bcap) {
+            if (g_fill.d_boxes) cudaFree(g_fill.d_boxes);
+            g_fill.d_boxes = nullptr;
+            if ((e = cudaMalloc(&g_fill.d_boxes, bytes)) != cudaSuccess) return e;
+            g_fill.bcap = fb.size();
+        }
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+        if ((e = cudaMemcpy(g_fill.d_boxes, fb.data(), bytes, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+        g_fill.table.resize(bytes);
+        std::memcpy(g_fill.table.data(), fb.data(), bytes);
+    }
+    const FillBox* tab = g_fill.d_boxes + (s_src ? nbox : 0);
+    FillGeom G;
+    for (int d = 0; d < 3; ++d) {
+        G.dlo[d] = g.domain_lo[d];
+        G.dhi[d] = g.domain_hi[d];
+        G.per[d] = g.is_periodic[d];
+        G.mlen[d] = g_fill.mlen[d];
+        G.dx[d] = g.dx[d];
+        G.plo[d] = g.prob_lo[d];
+    }
+    G.gran = g_fill.gran;
+    const int nc = NFLO + c_host_params().nspec;
+    dim3 grid((unsigned)((maxn + TPB - 1) / TPB), nbox);
+    copy_kernel<<<grid, TPB, 0, st>>>(tab, G, g_fill.d_owner, nc);
+    const bool any_phys = !(g.is_periodic[0] && g.is_periodic[1] && g.is_periodic[2]);
+    if (any_phys) {
+        const int ns = c_host_params().nspec;
+        for (int s = 1; s <= 3; ++s) {
+            if (ns <= 1) bc_kernel<1><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+            else if (ns <= 2) bc_kernel<2><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+            else if (ns <= 4) bc_kernel<4><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+            else if (ns <= 8) bc_kernel<8><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+            else bc_kernel<16><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+        }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mfg

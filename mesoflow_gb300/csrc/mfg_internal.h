@@ -1,0 +1,63 @@
+// Internal host/device interfaces shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "mfg_common.cuh"
+
+namespace mfg {
+
+// Per-cell scalars of prim_kernel (scratch over grow(bx, 3)).
+enum AuxComp { AUX_VX = 0, AUX_VY, AUX_VZ, AUX_PF, AUX_REIG, AUX_AOWN, AUX_GAM, NAUX };
+
+// Per-face scalars of face_kernel (scratch over growHi(bx, d, 1)).
+enum FsComp {
+    FS_FLAGS = 0,  // bit0: hyperbolic + viscous flux active, bit1: first-order IB fallback
+    FS_LAMBDA,     // LLF eigenvalue (orders 4, 5) or AUSM a_half (orders 1, 2)
+    FS_MH,         // AUSM M_half
+    FS_MODM,       // AUSM |M_half| with the entropy fix
+    FS_PH,         // AUSM p_half
+    FS_PL,         // AUSM left pressure
+    FS_PR,         // AUSM right pressure
+    FS_VIS,        // 3: viscous momentum terms tau_{d,a}
+    FS_VISE = FS_VIS + 3,   // 3: viscous work terms tau_{d,a} * facevel_a
+    FS_THERM = FS_VISE + 3, // heat-conduction term k dT/dn
+    NFS
+};
+
+// Everything the RHS kernels of one box need, passed by value.
+struct RhsBox {
+    int lo[3], hi[3];
+    double dx[3];
+    Fab sb, dsdt, sold, snew;
+    Fab uflux[3];
+    Fab aux;
+    Fab fs[3];
+    Fab flx[3];
+};
+
+const DevParams& c_host_params();
+
+cudaError_t upload_params(const DevParams& h);
+cudaError_t read_status(unsigned* v, bool clear);
+cudaError_t launch_rhs_box(const RhsBox& B, int stage, double dt, bool fast, cudaStream_t st);
+
+// Scratch sizes (doubles) for a box of the given valid extent.
+inline size_t aux_doubles(const int n[3]) {
+    return (size_t)(n[0] + 6) * (n[1] + 6) * (n[2] + 6) * NAUX;
+}
+inline size_t face_doubles(const int n[3], int d, int ncomp) {
+    return (size_t)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) * ncomp;
+}
+
+// Other kernels (mfg_ib.cu, mfg_fill.cu, mfg_step.cu)
+cudaError_t launch_chem_source(const mfg_box& b, cudaStream_t st);
+cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, double a, bool copy_first,
+                              const Fab& base, int ncomp, cudaStream_t st);
+cudaError_t launch_update_prims(const mfg_box& b, double* minp_slot, cudaStream_t st);
+cudaError_t launch_clip_species(const mfg_box& b, cudaStream_t st);
+cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st);
+
+cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g, int s_src, double time,
+                              cudaStream_t st);
+
+}  // namespace mfg

@@ -1,0 +1,155 @@
+// Device thermodynamics and transport for the three thermo families of the
+// reference's case plugins, evaluated from the parameter tables in constant
+// memory.  Operand order follows the plugins (sums over gas species in
+// ascending order, divisions where the plugins divide) so the FP64 results
+// track the reference's rounding.
+#pragma once
+#include "mfg_common.cuh"
+
+namespace mfg {
+
+extern __constant__ DevParams c_P;
+
+// Temperature from (rho, p, species).  Molar: ShockTube_N2/thermo.H:58-67,
+// catalystCylinder/thermo.H:54-63; mass-single: porousParticle/thermo.H:54-59;
+// background gas: rxnscheme example thermo.H:61-76.
+template <int NS>
+__device__ __forceinline__ double thermo_t(double rho, double pres, const double* spec) {
+    const DevParams& P = c_P;
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return pres / P.gas_R / rho;
+    double sum_ci = 0.0;
+    if (P.thermo_kind == MFG_THERMO_BG_GAS) {
+        double sum_ciMi = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) {
+                sum_ci += spec[s];
+                sum_ciMi += spec[s] * P.molwt[s];
+            }
+        double c_bg = (rho - sum_ciMi) / P.bg_molwt;
+        sum_ci += c_bg;
+        return pres / (sum_ci * kRU);
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) sum_ci += spec[s];
+    return pres / (sum_ci * P.R_univ);
+}
+
+// Pressure from (rho e, rho, species).
+template <int NS>
+__device__ __forceinline__ double thermo_p(double rhoe, double rho, const double* spec) {
+    const DevParams& P = c_P;
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return rhoe * (P.gamma_single - 1.0);
+    if (P.thermo_kind == MFG_THERMO_BG_GAS) {
+        double sum_ciMi = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) sum_ciMi += spec[s] * P.molwt[s];
+        double c_bg = (rho - sum_ciMi) / P.bg_molwt;
+        double cvs = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) cvs += P.cv[s] * spec[s];
+        cvs += P.cv[P.ngas] * c_bg;
+        double T = rhoe / cvs;
+        double p = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) p += spec[s] * kRU * T;
+        p += c_bg * kRU * T;
+        return p;
+    }
+    double cvs = 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) cvs += P.cv[s] * spec[s];
+    double T = rhoe / cvs;
+    double p = 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) p += spec[s] * P.R_univ * T;
+    return p;
+}
+
+// Mixture gamma (depends on composition only).
+template <int NS>
+__device__ __forceinline__ double thermo_gamma(double rho, const double* spec) {
+    const DevParams& P = c_P;
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return P.gamma_single;
+    double sum_ci = 0.0, term2 = 0.0;
+    if (P.thermo_kind == MFG_THERMO_BG_GAS) {
+        double sum_ciMi = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) sum_ciMi += spec[s] * P.molwt[s];
+        double c_bg = (rho - sum_ciMi) / P.bg_molwt;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) sum_ci += spec[s];
+        sum_ci += c_bg;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) term2 += (spec[s] / sum_ci) / (P.gamma[s] - 1.0);
+        term2 += (c_bg / sum_ci) / (P.gamma[P.ngas] - 1.0);
+        return 1.0 + 1.0 / term2;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) sum_ci += spec[s];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) term2 += (spec[s] / sum_ci) / (P.gamma[s] - 1.0);
+    return 1.0 + 1.0 / term2;
+}
+
+// Specific internal energy from (rho, p, species).
+template <int NS>
+__device__ __forceinline__ double thermo_e(double rho, double pres, const double* spec) {
+    const DevParams& P = c_P;
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return pres / (P.gamma_single - 1.0) / rho;
+    if (P.thermo_kind == MFG_THERMO_BG_GAS) {
+        double sum_ciMi = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) sum_ciMi += spec[s] * P.molwt[s];
+        double c_bg = (rho - sum_ciMi) / P.bg_molwt;
+        double temp = thermo_t<NS>(rho, pres, spec);
+        double scv = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) scv += P.cv[s] * spec[s];
+        scv += P.cv[P.ngas] * c_bg;
+        return scv * temp / rho;
+    }
+    if (P.energy_form == MFG_EFORM_MASS_CV) {
+        double sum_ci = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) sum_ci += spec[s];
+        double temp = thermo_t<NS>(rho, pres, spec);
+        double cvbar = 0.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.ngas) cvbar += P.cvmass[s] * (spec[s] / sum_ci);
+        return cvbar * temp;
+    }
+    double temp = thermo_t<NS>(rho, pres, spec);
+    double scv = 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) scv += P.cv[s] * spec[s];
+    return scv * temp / rho;
+}
+
+// Transport coefficient: constant, or gas*vfrac + solid*(1-vfrac).
+__device__ __forceinline__ double blend(int mode, double g, double s, double vf) {
+    return (mode == MFG_TRANSPORT_VFRAC_BLEND) ? (g * vf + s * (1.0 - vf)) : g;
+}
+
+// 2 d1 d2 / (d1 + d2 + 1e-30)  (compute_flux_3d.H:18-22)
+__device__ __forceinline__ double harmonic_mean(double d1, double d2) {
+    return 2.0 * d1 * d2 / (d1 + d2 + 1e-30);
+}
+
+}  // namespace mfg

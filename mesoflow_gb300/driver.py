@@ -1,0 +1,70 @@
+"""Single-level time stepping through the C ABI (the host loop of
+mflo::EvolveAMR, Source/mflo_evolve.cpp:18-89, for one level).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .level import Level
+
+
+class Mflo:
+    """Owns the device state of one level and advances it with
+    mfg_advance_level.  Mirrors mflo's single-level step: ComputeDt
+    (EstTimeStep, change_max = 1.1, stop_time clamp), Advance_coupled_strang,
+    update_primitive_vars, clip_neg_speciesconc, compute_residual_norms."""
+
+    def __init__(self, case, device="cuda", stream=None, with_dsdt=False, only_flow=False, clip=True):
+        import torch
+        self.lib = abi.load()
+        self.case = case
+        self.only_flow = only_flow
+        self.clip = clip
+        abi.check("mfg_init", self.lib.mfg_init(C.byref(case.params)))
+        self.level = Level(case.boxes, case.ncomp, backend="torch", device=device, with_dsdt=with_dsdt)
+        self.level.set_state(case.state)
+        self.desc = self.level.descriptors()
+        self.stream = stream if stream is not None else torch.cuda.current_stream().cuda_stream
+        self.time = 0.0
+        self.dt = 1e100
+        self.istep = 0
+        self.resnorms = np.zeros(case.ncomp)
+
+    def est_timestep(self):
+        out = C.c_double()
+        abi.check("mfg_est_timestep", self.lib.mfg_est_timestep(self.desc, len(self.case.boxes),
+                                                                 C.byref(self.case.geom), self.time,
+                                                                 C.byref(out), C.c_void_p(self.stream)))
+        return out.value
+
+    def compute_dt(self, stop_time=1e300):
+        """ComputeDt for one level (Source/mflo_timestep.cpp:18-50)."""
+        dt_new = min(self.est_timestep(), 1.1 * self.dt)
+        eps = 1e-3 * dt_new
+        if self.time + dt_new > stop_time - eps:
+            dt_new = stop_time - self.time
+        self.dt = dt_new
+        return dt_new
+
+    def advance(self, dt=None, norms=True):
+        if dt is None:
+            dt = self.compute_dt()
+        rn = (C.c_double * self.case.ncomp)()
+        abi.check("mfg_advance_level",
+                  self.lib.mfg_advance_level(self.desc, len(self.case.boxes), C.byref(self.case.geom), self.time,
+                                             dt, int(self.only_flow), int(self.clip), rn if norms else None,
+                                             C.c_void_p(self.stream)))
+        if norms:
+            self.resnorms = np.array(rn[:])
+        self.time += dt
+        self.istep += 1
+        return dt
+
+    def state(self):
+        return self.level.get_state(self.case.shape_zyx)
+
+    def status(self, clear=False):
+        v = C.c_uint32()
+        abi.check("mfg_status", self.lib.mfg_status(C.byref(v), int(clear)))
+        return v.value
