@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Benchmark: RK3 cell-updates/s of the plain per-box form on the 256^3
+immersed-boundary workload (seeded sphere pack, solid fraction 0.4,
+pressure-driven flow, FP64), one full step = mflo's single-level coarse step
+(fill patch, cut cells, three fused RHS + stage updates, chemistry sub-step,
+primitive refresh, clipping, residual norms) through mfg_advance_level.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs one independent replica per GPU (the path has no data exchange
+on one level of one GPU; replicas only), launched by torchrun.  The
+reference arm times the oracle (the CPU restatement of the reference's
+numerics, OpenMP over boxes) on a bounded sample of the same workload on the
+host cores.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK3 cell-updates/s (FP64 256^3 IB)"
+UNIT = "cell-updates/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+FP64_PEAK_TFLOPS = 1.256  # measured DFMA issue rate: 2 DFMA/clk/SM x 152 SMs x 2.07 GHz x 2 flop
+
+
+def workload_args(a):
+    return dict(n=a.n, order=a.order, max_grid=a.max_grid, seed=3, solid_frac=0.4)
+
+
+def make_case(a, n=None, max_grid=None):
+    from mesoflow_gb300 import cases
+    kw = workload_args(a)
+    if n is not None:
+        kw["n"] = n
+    if max_grid is not None:
+        kw["max_grid"] = max_grid
+    return cases.porous_ib(**kw)
+
+
+def workload_name(a):
+    return (f"porous_ib {a.n}^3 seeded sphere pack (radii 4-12 cells, solid 0.4, 2-cell smoothing), "
+            f"pressure-driven air, viscous, order_hyp={a.order}, {a.max_grid}^3 boxes")
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, idx):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(idx), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=4):
+    """The oracle (OpenMP build) on a bounded sample: the same workload
+    generator at n=128 with 32^3 boxes; returns (cell-updates/s, threads, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_run import OracleLevel
+    ns = 128
+    case = make_case(a, n=ns, max_grid=32)
+    o = OracleLevel(case, variant="omp")
+    dt = o.est_timestep()
+    o.advance(dt)  # warm-up
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        o.advance(dt)
+        k += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and k >= steps) or (steps is None and (el >= min_seconds or k >= max_steps)):
+            break
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cells = case.n_cell[0] * case.n_cell[1] * case.n_cell[2]
+    sample = (f"{ns}^3 instance of the same generator ({len(case.boxes)} boxes of 32^3), {k} RK3 steps after 1 "
+              f"warm-up, {el:.1f} s wall, OpenMP over boxes")
+    return cells * k / el, threads, sample
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    v, th, sample = cpu_port_time(a, steps=None)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "higher_is_better": True,
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(a)}, "scaling": "weak", "vs_baseline": None,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference cannot be built here (its AMReX submodule is not vendored, no MPI); "
+                    "this arm times the oracle, a line-by-line CPU restatement of its numerics"}
+    print(json.dumps(line))
+    return 0
+
+
+def algorithmic(kind, case, a, nlaunch_per_step):
+    """Algorithmic bytes per launch of a kernel kind (unique compulsory
+    traffic), for one box of max_grid^3 cells."""
+    B = a.max_grid
+    N = case.ncomp
+    Cadv = 5 + case.params.nspec
+    faces = (B + 1) * B * B
+    if kind == "flux":
+        # state components of the advected vector on the stencil extent, face scalars in, fluxes out
+        return 8.0 * (Cadv * (B + 6) * B * B + 14 * faces + Cadv * faces)
+    if kind == "face":
+        # conserved + species on the extent, velocities/T/vfrac around the face, face scalars out
+        return 8.0 * ((Cadv + 5) * (B + 6) * B * B + 14 * faces)
+    if kind == "update":
+        # fluxes of 3 directions in, sborder/s_old/s_new in, s_new out
+        return 8.0 * (3 * Cadv * faces + 4 * N * B ** 3)
+    if kind == "cutcell":
+        return 8.0 * (2 * N * B ** 3)
+    return 8.0 * 2 * N * B ** 3
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--order", type=int, default=2)
+    ap.add_argument("--max-grid", dest="max_grid", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    if a.impl == "reference":
+        return run_reference(a)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from mesoflow_gb300 import abi
+    from mesoflow_gb300.level import Level
+    lib = abi.load()
+    case = make_case(a)
+    abi.check("mfg_init", lib.mfg_init(C.byref(case.params)))
+    lev = Level(case.boxes, case.ncomp, backend="torch", device=f"cuda:{local}", with_dsdt=False)
+    lev.set_state(case.state)
+    desc = lev.descriptors()
+    stream = torch.cuda.current_stream()
+    st = C.c_void_p(stream.cuda_stream)
+    geom = C.byref(case.geom)
+    nb = len(case.boxes)
+    cells = lev.cells()
+    dt_c = C.c_double()
+    abi.check("mfg_est_timestep", lib.mfg_est_timestep(desc, nb, geom, 0.0, C.byref(dt_c), st))
+    dt = dt_c.value
+    rn = (C.c_double * case.ncomp)()
+
+    def step(t):
+        abi.check("mfg_advance_level", lib.mfg_advance_level(desc, nb, geom, t, dt, 0, 1, rn, st))
+
+    t = 0.0
+    for _ in range(a.warmup):
+        step(t)
+        t += dt
+    # ---- device-resident timed region -------------------------------------------
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    l0 = lib.mfg_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        step(t)
+        t += dt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.mfg_launch_count() - l0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if dist:
+        x = torch.tensor([ms], device="cuda")
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        ms = float(x.item())
+    value = cells * a.steps * world / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ----------------------------
+    host = [torch.empty_like(x, device="cpu").pin_memory() for x in lev.s_new]
+    for h, x in zip(host, lev.s_new):
+        h.copy_(x)
+    h2d = sum(x.numel() * 8 for x in lev.s_new)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(a.steps):
+        for h, x in zip(host, lev.s_new):
+            x.copy_(h, non_blocking=True)
+        step(t)
+        t += dt
+        for h, x in zip(host, lev.s_new):
+            h.copy_(x, non_blocking=True)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3)
+    if dist:
+        x = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        ms_e2e = float(x.item())
+    e2e = cells * a.steps * world / (ms_e2e / 1e3)
+
+    # ---- per-kernel timing (CUDA events on the launching stream) -----------------
+    lib.mfg_profile(1)
+    step(t)
+    kk = 16
+    kms = (C.c_double * kk)()
+    kcnt = (C.c_longlong * kk)()
+    nk = lib.mfg_profile_read(kms, kcnt, kk)
+    lib.mfg_profile(0)
+    kernels = {lib.mfg_profile_name(i).decode(): {"ms": kms[i], "launches": kcnt[i]} for i in range(nk) if kcnt[i]}
+    tot = sum(v["ms"] for v in kernels.values())
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    avg_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
+    peaks, src = read_peaks()
+    abytes = algorithmic(dom, case, a, kernels[dom]["launches"])
+    achieved = abytes / (avg_ms / 1e3) / 1e9
+    prof_path = os.path.join(ROOT, "profiles", "flux_traffic.json")
+    traffic = None
+    if os.path.exists(prof_path):
+        with open(prof_path) as f:
+            tr = json.load(f)
+        if tr.get("kernel") == dom and tr.get("order") == a.order:
+            traffic = tr.get("dram_bytes_per_launch_scaled")
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+            "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic, "peak_source": src,
+            "algorithmic_bytes_per_launch": abytes, "avg_launch_ms": avg_ms,
+            "share_of_step": kernels[dom]["ms"] / tot if tot else None}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": workload_name(a), "cells": cells, "boxes": nb, "order_hyp": a.order,
+                      "dt": dt, "l2": "inputs larger than L2 (state %.2f GB)" % (h2d / 1e9),
+                      "parallelism": f"replicas x{world}"},
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
+           "gpu_launches": launches, "clocks": clk, "roofline": roof,
+           "kernels_ms_per_step": {k: v["ms"] for k, v in kernels.items()},
+           "fp64_peak_tflops": FP64_PEAK_TFLOPS}
+    if rank == 0 and not a.no_cpu:
+        v, th, sample = cpu_port_time(a)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -283,6 +283,22 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom,
  * four reciprocals (flux_schemes.H:407-414) operation for operation. */
 int mfg_set_weno_mode(int fast);
 
+/* ---- diagnostics (no counterpart in the reference beyond BL_PROFILE) ------ */
+
+/* Enables (1) or disables (0) CUDA-event timing of every kernel launch and
+ * resets the accumulated times. */
+int mfg_profile(int enable);
+
+/* Accumulated milliseconds and launch counts per kernel kind (synchronizes);
+ * returns the number of kinds. */
+int mfg_profile_read(double* ms, long long* count, int nkinds);
+
+/* Name of a kernel kind of mfg_profile_read. */
+const char* mfg_profile_name(int kind);
+
+/* Total kernel launches issued by the library since it was loaded. */
+unsigned long long mfg_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

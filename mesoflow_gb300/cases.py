@@ -202,40 +202,44 @@ def taylor_green_mix(n=256, order=5, max_grid=64, seed=20261203, v0=10.0):
 
 def sphere_pack_vfrac(n, seed, solid_frac, rmin=4.0, rmax=12.0, smooth=True):
     """Fluid volume fraction of a seeded random pack of overlapping spheres
-    (radii uniform in [rmin, rmax] cells) grown until the solid fraction reaches
-    solid_frac; 8-corner sampling as the reference's initdata
-    (tests/ImmBoundary/subsonicCylinder/Prob.H:39-59), then a 2-cell box filter
-    and snapping of near-0/1 values so that pure cells stay exactly 0 or 1."""
+    (radii uniform in [rmin, rmax] cells, centres uniform in the domain), grown
+    until the solid fraction of the cell corners reaches solid_frac; 8-corner
+    sampling as the reference's initdata (tests/ImmBoundary/subsonicCylinder/
+    Prob.H:39-59), then a 2-cell box filter (one 3-point average per axis:
+    the 8-corner ramp of one cell widens to about two) and snapping of values within 1e-3 of 0 or 1, so that pure cells
+    stay exactly 0 or 1."""
     rng = np.random.default_rng(seed)
     nn = n + 1
     ax = np.arange(nn, dtype=np.float64)
-    solid_c = np.zeros((nn, nn, nn), dtype=bool)  # corner (k,j,i) inside a sphere
-    centers = []
-    while True:
+    solid_c = np.zeros((nn, nn, nn), dtype=bool)  # corner (k, j, i) inside a sphere
+    nsolid, target = 0, solid_frac * nn ** 3
+    while nsolid < target:
         c = rng.uniform(0, n, size=3)
         r = rng.uniform(rmin, rmax)
-        centers.append((c, r))
         lo = np.maximum(np.floor(c - r).astype(int), 0)
         hi = np.minimum(np.ceil(c + r).astype(int) + 1, nn)
-        zz, yy, xx = np.meshgrid(ax[lo[2]:hi[2]], ax[lo[1]:hi[1]], ax[lo[0]:hi[0]], indexing="ij")
-        inside = (xx - c[0]) ** 2 + (yy - c[1]) ** 2 + (zz - c[2]) ** 2 <= r * r
-        solid_c[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] |= inside
-        fluid = (~solid_c).astype(np.float64)
-        vf = 0.125 * sum(fluid[kk:kk + n, jj:jj + n, ii:ii + n] for kk in (0, 1) for jj in (0, 1) for ii in (0, 1))
-        if 1.0 - vf.mean() >= solid_frac:
-            break
+        if np.any(hi <= lo):
+            continue
+        dz = (ax[lo[2]:hi[2]] - c[2])[:, None, None] ** 2
+        dy = (ax[lo[1]:hi[1]] - c[1])[None, :, None] ** 2
+        dx = (ax[lo[0]:hi[0]] - c[0])[None, None, :] ** 2
+        inside = (dz + dy + dx) <= r * r
+        sl = (slice(lo[2], hi[2]), slice(lo[1], hi[1]), slice(lo[0], hi[0]))
+        nsolid += int(np.count_nonzero(inside & ~solid_c[sl]))
+        solid_c[sl] |= inside
+    fluid = (~solid_c).astype(np.float64)
+    vf = 0.125 * sum(fluid[kk:kk + n, jj:jj + n, ii:ii + n] for kk in (0, 1) for jj in (0, 1) for ii in (0, 1))
     if smooth:
-        for axis in range(3):  # separable 3-point average, applied twice: ~2-cell box filter
-            for _ in range(2):
-                pad = [(0, 0)] * 3
-                pad[axis] = (1, 1)
-                q = np.pad(vf, pad, mode="edge")
-                sl = [slice(None)] * 3
-                acc = 0.0
-                for o in range(3):
-                    sl[axis] = slice(o, o + n)
-                    acc = acc + q[tuple(sl)]
-                vf = acc / 3.0
+        for axis in range(3):
+            pad = [(0, 0)] * 3
+            pad[axis] = (1, 1)
+            q = np.pad(vf, pad, mode="edge")
+            sl = [slice(None)] * 3
+            acc = 0.0
+            for o in range(3):
+                sl[axis] = slice(o, o + n)
+                acc = acc + q[tuple(sl)]
+            vf = acc / 3.0
         vf[vf >= 0.999] = 1.0
         vf[vf <= 0.001] = 0.0
     return vf

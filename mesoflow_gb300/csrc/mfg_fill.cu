@@ -309,11 +309,15 @@ cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g,
     G.gran = g_fill.gran;
     const int nc = NFLO + c_host_params().nspec;
     dim3 grid((unsigned)((maxn + TPB - 1) / TPB), nbox);
-    copy_kernel<<<grid, TPB, 0, st>>>(tab, G, g_fill.d_owner, nc);
+    {
+        ProfScope ps(K_FILL_COPY, st);
+        copy_kernel<<<grid, TPB, 0, st>>>(tab, G, g_fill.d_owner, nc);
+    }
     const bool any_phys = !(g.is_periodic[0] && g.is_periodic[1] && g.is_periodic[2]);
     if (any_phys) {
         const int ns = c_host_params().nspec;
         for (int s = 1; s <= 3; ++s) {
+            ProfScope ps(K_FILL_BC, st);
             if (ns <= 1) bc_kernel<1><<<grid, TPB, 0, st>>>(tab, G, s, nc);
             else if (ns <= 2) bc_kernel<2><<<grid, TPB, 0, st>>>(tab, G, s, nc);
             else if (ns <= 4) bc_kernel<4><<<grid, TPB, 0, st>>>(tab, G, s, nc);

@@ -201,6 +201,7 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
         for (int d = 0; d < 3; ++d) g_wdir_dx[d] = g.dx[d];
     }
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
+    ProfScope ps(K_CUT, st);
     if (c_host_params().conj_ht) cht_avg_kernel<<<nb, TPB, 0, st>>>(c);
     const int ns = c_host_params().nspec;
     if (ns <= 1) cutcell_kernel<1><<<nb, TPB, 0, st>>>(c);

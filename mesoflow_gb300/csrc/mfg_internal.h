@@ -24,6 +24,24 @@ enum FsComp {
     NFS
 };
 
+// Kernel kinds of the launch counter / event profiler (mfg_prof.cu).
+enum KernelKind {
+    K_PRIM = 0, K_FACE, K_FLUX, K_UPDATE, K_FILL_COPY, K_FILL_BC, K_CUT, K_CHEM, K_PRIMS, K_CLIP,
+    K_RESNORM, K_TIMESTEP, K_COPY, K_COUNT
+};
+
+// Counts one launch; when profiling is on, brackets it with CUDA events on its stream.
+class ProfScope {
+  public:
+    ProfScope(int kind, cudaStream_t st);
+    ~ProfScope();
+
+  private:
+    int kind_;
+    cudaStream_t st_;
+    void* a_;
+};
+
 // Everything the RHS kernels of one box need, passed by value.
 struct RhsBox {
     int lo[3], hi[3];

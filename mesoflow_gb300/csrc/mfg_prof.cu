@@ -1,0 +1,97 @@
+// Launch counter and per-kernel CUDA-event timing (enabled on request), the
+// library's counterpart of the reference's BL_PROFILE regions.
+#include <vector>
+
+#include "mfg_internal.h"
+
+namespace mfg {
+namespace {
+
+const char* kNames[K_COUNT] = {"prim", "face", "flux", "update", "fill_copy", "fill_bc",
+                               "cutcell", "chem", "prims", "clip", "resnorm", "timestep", "copy"};
+
+struct Pending {
+    int kind;
+    cudaEvent_t a, b;
+};
+
+bool g_on = false;
+unsigned long long g_launches = 0;
+std::vector<Pending> g_pending;
+std::vector<cudaEvent_t> g_free;
+double g_ms[K_COUNT];
+long long g_cnt[K_COUNT];
+
+cudaEvent_t ev() {
+    if (!g_free.empty()) {
+        cudaEvent_t e = g_free.back();
+        g_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void drain() {
+    for (auto& p : g_pending) {
+        cudaEventSynchronize(p.b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        g_ms[p.kind] += ms;
+        g_cnt[p.kind] += 1;
+        g_free.push_back(p.a);
+        g_free.push_back(p.b);
+    }
+    g_pending.clear();
+}
+
+}  // namespace
+
+ProfScope::ProfScope(int kind, cudaStream_t st) : kind_(kind), st_(st), a_(nullptr) {
+    ++g_launches;
+    if (g_on) {
+        a_ = ev();
+        cudaEventRecord((cudaEvent_t)a_, st_);
+    }
+}
+
+ProfScope::~ProfScope() {
+    if (g_on && a_) {
+        cudaEvent_t b = ev();
+        cudaEventRecord(b, st_);
+        g_pending.push_back({kind_, (cudaEvent_t)a_, b});
+        if (g_pending.size() > 4096) drain();
+    }
+}
+
+}  // namespace mfg
+
+using namespace mfg;
+
+extern "C" {
+
+int mfg_profile(int enable) {
+    drain();
+    g_on = enable != 0;
+    for (int k = 0; k < K_COUNT; ++k) {
+        g_ms[k] = 0.0;
+        g_cnt[k] = 0;
+    }
+    return MFG_OK;
+}
+
+int mfg_profile_read(double* ms, long long* count, int nkinds) {
+    drain();
+    for (int k = 0; k < K_COUNT && k < nkinds; ++k) {
+        if (ms) ms[k] = g_ms[k];
+        if (count) count[k] = g_cnt[k];
+    }
+    return K_COUNT;
+}
+
+const char* mfg_profile_name(int kind) { return (kind >= 0 && kind < K_COUNT) ? kNames[kind] : ""; }
+
+unsigned long long mfg_launch_count(void) { return g_launches; }
+
+}  // extern "C"

@@ -526,18 +526,26 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
         nv *= (B.hi[e] - B.lo[e] + 1);
     }
     const int ord = c_host_params().order_hyp;
-    if (ord == 4 || ord == 5) prim_kernel<NS><<<blocks_for(ng), TPB, 0, st>>>(B);
+    if (ord == 4 || ord == 5) {
+        ProfScope ps(K_PRIM, st);
+        prim_kernel<NS><<<blocks_for(ng), TPB, 0, st>>>(B);
+    }
     for (int d = 0; d < 3; ++d) {
         int64_t nf = 1;
         for (int e = 0; e < 3; ++e) nf *= (B.hi[e] - B.lo[e] + 1 + (e == d));
-        face_kernel<NS><<<blocks_for(nf), TPB, 0, st>>>(B, d);
+        {
+            ProfScope ps(K_FACE, st);
+            face_kernel<NS><<<blocks_for(nf), TPB, 0, st>>>(B, d);
+        }
         dim3 g(blocks_for(nf), C);
+        ProfScope ps(K_FLUX, st);
         if (fast)
             flux_kernel<true><<<g, TPB, 0, st>>>(B, d);
         else
             flux_kernel<false><<<g, TPB, 0, st>>>(B, d);
     }
     dim3 gu(blocks_for(nv), N);
+    ProfScope ps(K_UPDATE, st);
     update_kernel<<<gu, TPB, 0, st>>>(B, stage, dt);
     return cudaGetLastError();
 }

@@ -163,8 +163,9 @@ __global__ void resnorm_kernel(Valid v, Fab Sn, Fab So, double a, double b, doub
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of(v, t, i, j, k);
-        double d = a * Sn(i, j, k, n) + b * So(i, j, k, n);
-        if (n < VFRAC) d *= So(i, j, k, VFRAC);
+        // LinComb then Multiply, rounded as the reference (no contraction)
+        double d = add(mul(a, Sn(i, j, k, n)), mul(b, So(i, j, k, n)));
+        if (n < VFRAC) d = mul(d, So(i, j, k, VFRAC));
         acc += d * d;
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -253,6 +254,7 @@ cudaError_t launch_chem_source(const mfg_box& b, cudaStream_t st) {
     Valid v = valid_of(b);
     Fab S = make_fab(b.s_new), D = make_fab(b.dsdt);
     const int ns = c_host_params().nspec;
+    ProfScope ps(K_CHEM, st);
     if (ns <= 1) chem_source_kernel<1><<<nblocks(v.n), TPB, 0, st>>>(v, S, D);
     else if (ns <= 2) chem_source_kernel<2><<<nblocks(v.n), TPB, 0, st>>>(v, S, D);
     else if (ns <= 4) chem_source_kernel<4><<<nblocks(v.n), TPB, 0, st>>>(v, S, D);
@@ -265,6 +267,7 @@ cudaError_t launch_chem_substep(const mfg_box& b, double dt, cudaStream_t st) {
     Valid v = valid_of(b);
     Fab So = make_fab(b.s_old), Sn = make_fab(b.s_new);
     const int ns = c_host_params().nspec, nc = NFLO + ns;
+    ProfScope ps(K_CHEM, st);
     if (ns <= 1) chem_substep_kernel<1><<<nblocks(v.n), TPB, 0, st>>>(v, So, Sn, dt, nc);
     else if (ns <= 2) chem_substep_kernel<2><<<nblocks(v.n), TPB, 0, st>>>(v, So, Sn, dt, nc);
     else if (ns <= 4) chem_substep_kernel<4><<<nblocks(v.n), TPB, 0, st>>>(v, So, Sn, dt, nc);
@@ -277,6 +280,7 @@ cudaError_t launch_update_prims(const mfg_box& b, double*, cudaStream_t st) {
     Valid v = valid_of(b);
     Fab S = make_fab(b.s_new);
     const int ns = c_host_params().nspec;
+    ProfScope ps(K_PRIMS, st);
     if (ns <= 1) prims_kernel<1><<<nblocks(v.n), TPB, 0, st>>>(v, S);
     else if (ns <= 2) prims_kernel<2><<<nblocks(v.n), TPB, 0, st>>>(v, S);
     else if (ns <= 4) prims_kernel<4><<<nblocks(v.n), TPB, 0, st>>>(v, S);
@@ -287,6 +291,7 @@ cudaError_t launch_update_prims(const mfg_box& b, double*, cudaStream_t st) {
 
 cudaError_t launch_clip_species(const mfg_box& b, cudaStream_t st) {
     Valid v = valid_of(b);
+    ProfScope ps(K_CLIP, st);
     clip_kernel<<<nblocks(v.n), TPB, 0, st>>>(v, make_fab(b.s_new), c_host_params().nspec);
     return cudaGetLastError();
 }
@@ -297,6 +302,7 @@ cudaError_t launch_resnorm_box(const mfg_box& b, double dt, double* partial, dou
     const int nc = NFLO + c_host_params().nspec;
     int nblk = (int)std::min<int64_t>(1024, (v.n + TPB - 1) / TPB);
     dim3 g(nblk, nc);
+    ProfScope ps(K_RESNORM, st);
     resnorm_kernel<<<g, TPB, 0, st>>>(v, make_fab(b.s_new), make_fab(b.s_old), 1.0 / dt, -1.0 / dt, partial, nblk);
     resnorm_final_kernel<<<nc, 32, 0, st>>>(partial, nblk, acc);
     return cudaGetLastError();
@@ -306,6 +312,7 @@ cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st) {
     Valid v = valid_of(b);
     Fab S = make_fab(b.s_new);
     const int ns = c_host_params().nspec;
+    ProfScope ps(K_TIMESTEP, st);
     if (ns <= 1) timestep_kernel<1><<<nblocks(v.n), TPB, 0, st>>>(v, S, acc2);
     else if (ns <= 2) timestep_kernel<2><<<nblocks(v.n), TPB, 0, st>>>(v, S, acc2);
     else if (ns <= 4) timestep_kernel<4><<<nblocks(v.n), TPB, 0, st>>>(v, S, acc2);
@@ -318,6 +325,7 @@ cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, 
                               const Fab& base, int ncomp, cudaStream_t st) {
     Valid v = valid_of(b);
     dim3 g(nblocks(v.n), ncomp);
+    ProfScope ps(K_COPY, st);
     axpy_kernel<<<g, TPB, 0, st>>>(v, dst, src, a, copy_first ? 1 : 0, base, ncomp);
     return cudaGetLastError();
 }

@@ -11,7 +11,9 @@ ODIR = os.path.join(ROOT, "oracle")
 
 
 def build():
-    subprocess.run(["make", "-s", "-C", ODIR], check=True)
+    r = subprocess.run(["make", "-s", "-C", ODIR], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
 
 
 def load(variant="strict"):
