@@ -248,7 +248,7 @@ def sphere_pack_vfrac(n, seed, solid_frac, rmin=4.0, rmax=12.0, smooth=True):
 def porous_ib(n=256, order=2, max_grid=64, seed=3, solid_frac=0.4, dx=2e-6, p_out=1e5, dp_rel=1e-3):
     """Pressure-driven flow through a seeded sphere pack (models/porousParticle
     pattern): air (W = 0.0289, gamma 1.4, p = rho R_air T), mu = 1e-5,
-    k = 0.014, D = 1e-5, species_in_solid = 0; x: pressure inlet
+    k = 0.014, D = 1e-5, species_in_solid = 0, cfl 0.1; x: pressure inlet
     p_in = (1 + dp_rel) p_out / pressure outlet p_out (ext_dir), y/z: walls."""
     P = _base_params(1)
     P.thermo_kind = abi.THERMO_MASS_SINGLE
@@ -262,7 +262,7 @@ def porous_ib(n=256, order=2, max_grid=64, seed=3, solid_frac=0.4, dx=2e-6, p_ou
     P.diff_gas[0] = 1e-5
     P.species_in_solid = 0
     P.order_hyp = order
-    P.cfl = 0.4
+    P.cfl = 0.1  # models/porousParticle/inputs (mflo.cfl); 0.4 per direction is unstable in 3D
     T = 300.0
     p_in = p_out * (1.0 + dp_rel)
     rho_in = p_in / (P.gas_R * T)
