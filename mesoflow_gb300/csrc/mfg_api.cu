@@ -10,7 +10,8 @@
 
 namespace mfg {
 
-cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, cudaStream_t st);
+cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, int* list,
+                                unsigned* count, cudaStream_t st);
 cudaError_t launch_chem_substep(const mfg_box& b, double dt, cudaStream_t st);
 cudaError_t launch_resnorm_box(const mfg_box& b, double dt, double* partial, double* acc, cudaStream_t st);
 void fill_release();
@@ -94,6 +95,7 @@ RhsBox make_rhs_box(const mfg_box& b, const mfg_geom& g, double* base) {
         B.lo[d] = b.lo[d];
         B.hi[d] = b.hi[d];
         B.dx[d] = g.dx[d];
+        B.idx[d] = 1.0 / g.dx[d];
         n[d] = b.hi[d] - b.lo[d] + 1;
     }
     B.sb = make_fab(b.sborder);
@@ -183,6 +185,14 @@ int mfg_init(const mfg_params* p) {
         h.cv[s] = R / (p->gamma[s] - 1.0);
         if (s < p->ngas && p->molwt[s] != 0.0) h.cvmass[s] = R / (p->gamma[s] - 1.0) / p->molwt[s];
     }
+    auto hmean = [](double d1, double d2) { return 2.0 * d1 * d2 / (d1 + d2 + 1e-30); };
+    h.visc_hm = hmean(p->visc_gas, p->visc_gas);
+    h.cond_hm = hmean(p->cond_gas, p->cond_gas);
+    for (int s = 0; s < MFG_MAX_SPECIES; ++s) h.diff_hm[s] = hmean(p->diff_gas[s], p->diff_gas[s]);
+    if (p->thermo_kind == MFG_THERMO_MASS_SINGLE) {
+        h.g_gm1 = p->gamma_single / (p->gamma_single - 1.0);
+        h.astar_fac = (2.0 * (p->gamma_single - 1.0)) / (p->gamma_single + 1.0);
+    }
     h.visc_mode = p->visc_mode;
     h.cond_mode = p->cond_mode;
     h.visc_gas = p->visc_gas;
@@ -254,19 +264,20 @@ int mfg_cutcells(const mfg_box* boxes, int nbox, const mfg_geom* geom, double ti
     if (rc) return rc;
     if (!geom) return MFG_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    double* tcht = nullptr;
-    if (g_hp.conj_ht) {
-        size_t need = 0;
-        for (int b = 0; b < nbox; ++b) {
-            size_t n = 1;
-            for (int d = 0; d < 3; ++d) n *= (size_t)(boxes[b].hi[d] - boxes[b].lo[d] + 1);
-            need = std::max(need, n);
-        }
-        if (pool_reserve(need * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
-        tcht = reinterpret_cast<double*>(g_pool.p);
+    size_t need = 0;
+    for (int b = 0; b < nbox; ++b) {
+        size_t n = 1;
+        for (int d = 0; d < 3; ++d) n *= (size_t)(boxes[b].hi[d] - boxes[b].lo[d] + 1);
+        need = std::max(need, n);
     }
+    // scratch: [count | cut-cell list | CHT temperatures]
+    const size_t list_bytes = ((need * sizeof(int) + 255) / 256) * 256;
+    if (pool_reserve(256 + list_bytes + need * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
+    unsigned* count = reinterpret_cast<unsigned*>(g_pool.p);
+    int* list = reinterpret_cast<int*>(g_pool.p + 256);
+    double* tcht = reinterpret_cast<double*>(g_pool.p + 256 + list_bytes);
     for (int b = 0; b < nbox; ++b)
-        if (launch_cutcells_box(boxes[b], *geom, tcht, st) != cudaSuccess) return MFG_ERR_CUDA;
+        if (launch_cutcells_box(boxes[b], *geom, tcht, list, count, st) != cudaSuccess) return MFG_ERR_CUDA;
     return MFG_OK;
 }
 

@@ -38,6 +38,10 @@ struct DevParams {
     double visc_gas, visc_solid, cond_gas, cond_solid;
     int diff_mode[MAXS];
     double diff_gas[MAXS], diff_solid[MAXS];
+    // face coefficients of constant transport: harmonic_mean(g, g), evaluated once
+    double visc_hm, cond_hm, diff_hm[MAXS];
+    // gamma/(gamma-1) and 2(gamma-1)/(gamma+1) of the mass-single family
+    double g_gm1, astar_fac;
     int order_hyp, do_ns, species_in_solid, conj_ht;
     double dissfactor, solid_temp, cfl;
     int chem_on, nreact;
@@ -98,5 +102,20 @@ __device__ __forceinline__ void raise_status(unsigned bits) { atomicOr(&g_status
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// Reciprocal of a positive, finite, normal x: the hardware approximation
+// (PTX rcp.approx.ftz.f64) refined by two Newton-Raphson steps
+// r <- r + r (1 - x r), each of which squares the relative error, so the
+// result is within one ulp of 1/x.  Four FMAs instead of a full IEEE
+// division; used where the reference divides by a positive weight sum or a
+// squared distance and the result only enters tolerance-checked sums.
+__device__ __forceinline__ double rcp_pos(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
 
 }  // namespace mfg

@@ -10,9 +10,14 @@
 // all over the vfrac == 1 cells of the 5^3 neighbourhood; the conserved
 // variables are then re-derived from the primitives.
 //
-// Each neighbour's weight 1/(d^2 + 1e-40) is computed once and shared by all
-// interpolated components (the reference divides per component); the
+// Work layout: a compaction pass lists the box's cut cells (one atomic per
+// warp), then a fixed grid of threads walks the list, one cut cell per thread,
+// so no lane idles on pure fluid or solid cells.  Each neighbour's weight
+// 1/(d^2 + 1e-40) is computed once (Newton-refined reciprocal) and shared by
+// all interpolated components (the reference divides per component); the
 // Dirichlet weights depend only on the grid and come from a constant table.
+#include <algorithm>
+
 #include "mfg_internal.h"
 #include "mfg_physics.cuh"
 
@@ -58,16 +63,43 @@ __global__ void cht_avg_kernel(CutBox c) {
     c.tcht[t] = sum / 26.0;
 }
 
-template <int NS>
-__global__ void __launch_bounds__(TPB) cutcell_kernel(CutBox c) {
+// Appends the linear index of every cut cell (0 < vfrac < 1) of the box to list.
+__global__ void cut_list_kernel(CutBox c, int* __restrict__ list, unsigned* __restrict__ count) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= c.n) return;
+    bool cut = false;
+    if (t < c.n) {
+        int i, j, k;
+        cell_of(c, t, i, j, k);
+        const double vf = c.S(i, j, k, VFRAC);
+        cut = vf > 0.0 && vf < 1.0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, cut);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    unsigned base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    if (cut) list[base + __popc(m & ((1u << lane) - 1u))] = (int)t;
+}
+
+template <int NS>
+__device__ void cutcell_one(const CutBox& c, int64_t t);
+
+template <int NS>
+__global__ void __launch_bounds__(TPB) cutcell_kernel(CutBox c, const int* __restrict__ list,
+                                                      const unsigned* __restrict__ count) {
+    const unsigned n = *count;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+        cutcell_one<NS>(c, list[w]);
+}
+
+template <int NS>
+__device__ void cutcell_one(const CutBox& c, int64_t t) {
     int i, j, k;
     cell_of(c, t, i, j, k);
     const Fab& S = c.S;
     const int64_t o = S.off(i, j, k);
     const double vf = S.p[o + VFRAC * S.ns];
-    if (!(vf > 0.0 && vf < 1.0)) return;
     const DevParams& P = c_P;
     const double* V = S.p + VFRAC * S.ns;
 
@@ -107,7 +139,7 @@ __global__ void __launch_bounds__(TPB) cutcell_kernel(CutBox c) {
                     swd += wd;
                 }
                 const double a = l * dxnd[0] - xpn[0], b = m * dxnd[1] - xpn[1], e = n * dxnd[2] - xpn[2];
-                const double wn = 1.0 / (((a * a + b * b) + e * e) + kTiny2);
+                const double wn = rcp_pos(((a * a + b * b) + e * e) + kTiny2);
                 sp += S.p[q + PRES * S.ns] * wn;
                 st += S.p[q + TEMP * S.ns] * wn;
                 sr += S.p[q + DENS * S.ns] * wn;
@@ -172,7 +204,8 @@ double g_wdir_dx[3] = {-1.0, -1.0, -1.0};
 
 }  // namespace
 
-cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, cudaStream_t st) {
+cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, int* list,
+                                unsigned* count, cudaStream_t st) {
     CutBox c;
     c.n = 1;
     for (int d = 0; d < 3; ++d) {
@@ -203,12 +236,16 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
     ProfScope ps(K_CUT, st);
     if (c_host_params().conj_ht) cht_avg_kernel<<<nb, TPB, 0, st>>>(c);
+    cudaMemsetAsync(count, 0, sizeof(unsigned), st);
+    cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count);
+    // a fixed grid walks the list (its length stays on the device)
+    const unsigned ng = (unsigned)std::min<int64_t>(nb, 152 * 8);
     const int ns = c_host_params().nspec;
-    if (ns <= 1) cutcell_kernel<1><<<nb, TPB, 0, st>>>(c);
-    else if (ns <= 2) cutcell_kernel<2><<<nb, TPB, 0, st>>>(c);
-    else if (ns <= 4) cutcell_kernel<4><<<nb, TPB, 0, st>>>(c);
-    else if (ns <= 8) cutcell_kernel<8><<<nb, TPB, 0, st>>>(c);
-    else cutcell_kernel<16><<<nb, TPB, 0, st>>>(c);
+    if (ns <= 1) cutcell_kernel<1><<<ng, TPB, 0, st>>>(c, list, count);
+    else if (ns <= 2) cutcell_kernel<2><<<ng, TPB, 0, st>>>(c, list, count);
+    else if (ns <= 4) cutcell_kernel<4><<<ng, TPB, 0, st>>>(c, list, count);
+    else if (ns <= 8) cutcell_kernel<8><<<ng, TPB, 0, st>>>(c, list, count);
+    else cutcell_kernel<16><<<ng, TPB, 0, st>>>(c, list, count);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,7 @@ class ProfScope {
 struct RhsBox {
     int lo[3], hi[3];
     double dx[3];
+    double idx[3];  // 1/dx
     Fab sb, dsdt, sold, snew;
     Fab uflux[3];
     Fab aux;

@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
 #pragma unroll
     for (int q = 0; q < NFS; ++q) fs[q] = 0.0;
     fs[FS_FLAGS] = (double)((active ? 1 : 0) | ((P.do_ns && fallback) ? 2 : 0));
+    double uL[NCONS + NS], uR[NCONS + NS];  // AUSM+-up face states (orders 1, 2)
 
     if (active) {
         const int ord = P.order_hyp;
@@ -236,7 +237,6 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
             fs[FS_LAMBDA] = fmax(aL, aR) + veln;
         } else {
             // AUSM+-up (flux_schemes.H:185-310) on first- or second-order states
-            double uL[NCONS + NS], uR[NCONS + NS];
             const int nc = NCONS + P.nspec;
 #pragma unroll
             for (int c = 0; c < NCONS + NS; ++c) {
@@ -253,8 +253,9 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
                 }
             }
             const double rL = uL[RHO], rR = uR[RHO];
-            const double vxL = uL[RHOU] / rL, vyL = uL[RHOV] / rL, vzL = uL[RHOW] / rL;
-            const double vxR = uR[RHOU] / rR, vyR = uR[RHOV] / rR, vzR = uR[RHOW] / rR;
+            const double irL = 1.0 / rL, irR = 1.0 / rR;
+            const double vxL = uL[RHOU] * irL, vyL = uL[RHOV] * irL, vzL = uL[RHOW] * irL;
+            const double vxR = uR[RHOU] * irR, vyR = uR[RHOV] * irR, vzR = uR[RHOW] * irR;
             const double kL = (vxL * vxL + vyL * vyL) + vzL * vzL;
             const double kR = (vxR * vxR + vyR * vyR) + vzR * vzR;
             const double pL = thermo_p<NS>(uL[RHOE] - (0.5 * rL) * kL, rL, uL + NCONS);
@@ -262,20 +263,22 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
             const double gL = thermo_gamma<NS>(rL, uL + NCONS), gR = thermo_gamma<NS>(rR, uR + NCONS);
             const double vL = (d == 0) ? vxL : (d == 1) ? vyL : vzL;
             const double vR = (d == 0) ? vxR : (d == 1) ? vyR : vzR;
-            const double HL = (gL / (gL - 1.0)) * (pL / rL) + 0.5 * kL;
-            const double HR = (gR / (gR - 1.0)) * (pR / rR) + 0.5 * kR;
+            const bool cg = P.thermo_kind == MFG_THERMO_MASS_SINGLE;
+            const double HL = (cg ? P.g_gm1 : gL / (gL - 1.0)) * (pL * irL) + 0.5 * kL;
+            const double HR = (cg ? P.g_gm1 : gR / (gR - 1.0)) * (pR * irR) + 0.5 * kR;
             const double rho_half = 0.5 * (rL + rR);
-            double as2 = ((2.0 * (gL - 1.0)) / (gL + 1.0)) * HL;
+            double as2 = (cg ? P.astar_fac : (2.0 * (gL - 1.0)) / (gL + 1.0)) * HL;
             const double ahL = as2 / fmax(sqrt(as2), fabs(vL));
-            as2 = ((2.0 * (gR - 1.0)) / (gR + 1.0)) * HR;
+            as2 = (cg ? P.astar_fac : (2.0 * (gR - 1.0)) / (gR + 1.0)) * HR;
             const double ahR = as2 / fmax(sqrt(as2), fabs(vR));
             const double ah = fmin(ahL, ahR);
-            const double ML = vL / ah, MR = vR / ah;
+            const double iah = 1.0 / ah;
+            const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
-            const double Mb2 = (0.5 * (vL * vL + vR * vR)) / (ah * ah);
+            const double Mb2 = (0.5 * (vL * vL + vR * vR)) * (iah * iah);
             const double Mo = sqrt(fmin(1.0, fmax(Mb2, 0.3 * 0.3)));
             const double fa = Mo * (2.0 - Mo);
-            Mh = Mh - (((0.25 / fa) * fmax(1.0 - Mb2, 0.0)) * (pR - pL)) / ((rho_half * ah) * ah);
+            Mh = Mh - (((0.25 / fa) * fmax(1.0 - Mb2, 0.0)) * (pR - pL)) * ((iah * iah) / rho_half);
             double modM = fabs(Mh);
             if (modM <= 0.3) modM = (Mh * Mh + 0.3 * 0.3) / (2.0 * 0.3);
             const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
@@ -293,15 +296,15 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
         const double* V0 = S.p + VELX * S.ns;
         const double* V1 = S.p + VELY * S.ns;
         const double* V2 = S.p + VELZ * S.ns;
-        const double dxs = B.dx[d], dx1 = B.dx[t1], dx2 = B.dx[t2];
+        const double ids = B.idx[d], ih1 = 0.5 * B.idx[t1], ih2 = 0.5 * B.idx[t2];
         double g[3][3];  // g[component][0: normal, 1: trans1, 2: trans2]
         const double* Vc[3] = {V0, V1, V2};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const double* V = Vc[a];
-            g[a][0] = (V[oR] - V[oL]) / dxs;
-            g[a][1] = (0.5 * (V[oL + st1] + V[oR + st1]) - 0.5 * (V[oL - st1] + V[oR - st1])) / (2.0 * dx1);
-            g[a][2] = (0.5 * (V[oL + st2] + V[oR + st2]) - 0.5 * (V[oL - st2] + V[oR - st2])) / (2.0 * dx2);
+            g[a][0] = (V[oR] - V[oL]) * ids;
+            g[a][1] = (0.5 * (V[oL + st1] + V[oR + st1]) - 0.5 * (V[oL - st1] + V[oR - st1])) * ih1;
+            g[a][2] = (0.5 * (V[oL + st2] + V[oR + st2]) - 0.5 * (V[oL - st2] + V[oR - st2])) * ih2;
         }
         // gradient along Cartesian axis x/y/z is the entry whose sweep role maps to it
         const int gx = (d == 0) ? 0 : (d == 1) ? 2 : 1;
@@ -311,9 +314,10 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
         const double dvdx = g[1][gx], dvdy = g[1][gy], dvdz = g[1][gz];
         const double dwdx = g[2][gx], dwdy = g[2][gy], dwdz = g[2][gz];
         // viscosity always from cells (i,j,k) and (i-1,j,k) (compute_flux_3d.H:179)
-        const double* vfr = vf;
-        const double mu = harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vfr[oR]),
-                                        blend(P.visc_mode, P.visc_gas, P.visc_solid, vfr[oR - 1]));
+        const double mu = (P.visc_mode == MFG_TRANSPORT_CONST)
+                              ? P.visc_hm
+                              : harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR]),
+                                              blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR - 1]));
         const double delu = (dudx + dvdy) + dwdz;
         double tau[3][3];
         tau[0][0] = mu * (2.0 * dudx - kTwo3rd * delu);
@@ -335,10 +339,56 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
     }
     if (P.do_ns) {
         // heat conduction (compute_flux_3d.H:373-374), conductivity from (i,j,k),(i-1,j,k)
-        const double kc = harmonic_mean(blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR]),
-                                        blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR - 1]));
+        const double kc = (P.cond_mode == MFG_TRANSPORT_CONST)
+                              ? P.cond_hm
+                              : harmonic_mean(blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR]),
+                                              blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR - 1]));
         const double* T = S.p + TEMP * S.ns;
-        fs[FS_THERM] = kc * ((T[oR] - T[oL]) / B.dx[d]);
+        fs[FS_THERM] = kc * ((T[oR] - T[oL]) * B.idx[d]);
+    }
+    if (P.do_ns && P.order_hyp <= 2) {
+        // AUSM+-up: the face thread holds the face states and the scheme scalars,
+        // so it writes every component's complete flux (no per-component pass).
+        const Fab& O = B.flx[d];
+        const int64_t qo = O.off(f.i, f.j, f.k);
+        const Fab& U = B.uflux[d];
+        const int64_t qu = U.p ? U.off(f.i, f.j, f.k) : 0;
+#pragma unroll
+        for (int c = 0; c < NCONS + NS; ++c) {
+            if (c >= NCONS + P.nspec) break;
+            const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+            double F = 0.0;
+            if (active) {
+                double fL = uL[c], fR = uR[c];
+                if (c == RHOE) {
+                    fL = uL[c] + fs[FS_PL];
+                    fR = uR[c] + fs[FS_PR];
+                }
+                double fh = ((0.5 * fs[FS_MH]) * (fL + fR) - (0.5 * fs[FS_MODM]) * (fR - fL)) * fs[FS_LAMBDA];
+                if (c == 1 + d) fh += fs[FS_PH];
+                F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
+                if (c >= RHOU && c <= RHOW) F -= fs[FS_VIS + c - 1];
+                if (c == RHOE) {
+                    F -= fs[FS_VISE + 0];
+                    F -= fs[FS_VISE + 1];
+                    F -= fs[FS_VISE + 2];
+                }
+            }
+            if (c == RHOE) F -= fs[FS_THERM];
+            if (c >= NCONS) {
+                const int s = c - NCONS;
+                const double Dh = (P.diff_mode[s] == MFG_TRANSPORT_CONST)
+                                      ? P.diff_hm[s]
+                                      : harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oL]),
+                                                      blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oR]));
+                F -= (Dh * (S.p[oR + sc * S.ns] - S.p[oL + sc * S.ns])) * B.idx[d];
+            }
+            O.p[qo + c * O.ns] = F;
+            if (U.p) U.p[qu + sc * U.ns] = F;
+        }
+        if (U.p)
+            for (int z = NCONS; z < NFLO; ++z) U.p[qu + z * U.ns] = 0.0;
+        return;
     }
     const Fab& F = B.fs[d];
     const int64_t q = F.off(f.i, f.j, f.k);
@@ -448,9 +498,11 @@ __global__ void __launch_bounds__(TPB) flux_kernel(RhsBox B, int d) {
         // species diffusion (compute_flux_3d.H:425-428)
         const int s = c - NCONS;
         const double* vfp = S.p + VFRAC * S.ns;
-        const double Dh = harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oL]),
-                                        blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oR]));
-        F -= (Dh * (u[oR] - u[oL])) / B.dx[d];
+        const double Dh = (P.diff_mode[s] == MFG_TRANSPORT_CONST)
+                              ? P.diff_hm[s]
+                              : harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oL]),
+                                              blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oR]));
+        F -= (Dh * (u[oR] - u[oL])) * B.idx[d];
     }
     const Fab& O = B.flx[d];
     O.p[O.off(f.i, f.j, f.k) + c * O.ns] = F;
@@ -483,8 +535,8 @@ __global__ void __launch_bounds__(TPB) update_kernel(RhsBox B, int stage, double
         const int64_t ox = Fx.off(x.i, x.j, x.k) + c * Fx.ns;
         const int64_t oy = Fy.off(x.i, x.j, x.k) + c * Fy.ns;
         const int64_t oz = Fz.off(x.i, x.j, x.k) + c * Fz.ns;
-        ds = ((Fx.p[ox] - Fx.p[ox + 1]) / B.dx[0] + (Fy.p[oy] - Fy.p[oy + Fy.js]) / B.dx[1]) +
-             (Fz.p[oz] - Fz.p[oz + Fz.ks]) / B.dx[2];
+        ds = ((Fx.p[ox] - Fx.p[ox + 1]) * B.idx[0] + (Fy.p[oy] - Fy.p[oy + Fy.js]) * B.idx[1]) +
+             (Fz.p[oz] - Fz.p[oz + Fz.ks]) * B.idx[2];
         ds = ds + 0.0;  // + source (compute_fluid_source is zero)
     }
     const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
@@ -537,6 +589,7 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
             ProfScope ps(K_FACE, st);
             face_kernel<NS><<<blocks_for(nf), TPB, 0, st>>>(B, d);
         }
+        if (c_host_params().do_ns && ord <= 2) continue;  // the face kernel wrote the fluxes
         dim3 g(blocks_for(nf), C);
         ProfScope ps(K_FLUX, st);
         if (fast)
