@@ -139,6 +139,14 @@ int run_rhs(const mfg_box* boxes, int nbox, const mfg_geom* geom, int stage, dou
 
 const DevParams& c_host_params() { return g_hp; }
 
+// Shared with the allocation-free entry point (mfg_noalloc.cu).
+int validate_boxes(const mfg_box* boxes, int nbox, bool need_sb, bool need_dsdt, bool need_old, bool need_new) {
+    return check_boxes(boxes, nbox, need_sb, need_dsdt, need_old, need_new);
+}
+size_t rhs_box_scratch_doubles(const int n[3]) { return rhs_scratch_doubles(n); }
+RhsBox layout_rhs_box(const mfg_box& b, const mfg_geom& g, double* base) { return make_rhs_box(b, g, base); }
+bool weno_fast_mode() { return g_fast_weno; }
+
 }  // namespace mfg
 
 using namespace mfg;
@@ -192,6 +200,7 @@ int mfg_init(const mfg_params* p) {
     if (p->thermo_kind == MFG_THERMO_MASS_SINGLE) {
         h.g_gm1 = p->gamma_single / (p->gamma_single - 1.0);
         h.astar_fac = (2.0 * (p->gamma_single - 1.0)) / (p->gamma_single + 1.0);
+        h.gm1_single = p->gamma_single - 1.0;
     }
     h.visc_mode = p->visc_mode;
     h.cond_mode = p->cond_mode;

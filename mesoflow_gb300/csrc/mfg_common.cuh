@@ -41,7 +41,7 @@ struct DevParams {
     // face coefficients of constant transport: harmonic_mean(g, g), evaluated once
     double visc_hm, cond_hm, diff_hm[MAXS];
     // gamma/(gamma-1) and 2(gamma-1)/(gamma+1) of the mass-single family
-    double g_gm1, astar_fac;
+    double g_gm1, astar_fac, gm1_single;
     int order_hyp, do_ns, species_in_solid, conj_ht;
     double dissfactor, solid_temp, cfl;
     int chem_on, nreact;
@@ -102,6 +102,12 @@ __device__ __forceinline__ void raise_status(unsigned bits) { atomicOr(&g_status
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// Volume-fraction tests on the integer pipe: for v >= 0 the IEEE order of
+// doubles is the order of their bit patterns, so v < 1 and v == 1 need no
+// FP64 compare (the FP64 pipe is the bottleneck of these kernels).
+__device__ __forceinline__ bool below_one(double v) { return __double_as_longlong(v) < 0x3FF0000000000000LL; }
+__device__ __forceinline__ bool is_one(double v) { return __double_as_longlong(v) == 0x3FF0000000000000LL; }
 
 // Reciprocal of a positive, finite, normal x: the hardware approximation
 // (PTX rcp.approx.ftz.f64) refined by two Newton-Raphson steps

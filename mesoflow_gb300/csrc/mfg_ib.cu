@@ -129,7 +129,7 @@ __device__ void cutcell_one(const CutBox& c, int64_t t) {
         for (int m = -SG; m <= SG; ++m)
             for (int l = -SG; l <= SG; ++l) {
                 const int64_t q = o + l + m * S.js + n * S.ks;
-                if (V[q] != 1.0) continue;
+                if (!is_one(V[q])) continue;
                 const int w = (l + SG) + SW * ((m + SG) + SW * (n + SG));
                 if (!(l == 0 && m == 0 && n == 0)) {
                     const double wd = c_wdir[w];

@@ -56,6 +56,13 @@ struct RhsBox {
 
 const DevParams& c_host_params();
 
+// Box validation, scratch size and scratch layout of the RHS (mfg_api.cu).
+int validate_boxes(const mfg_box* boxes, int nbox, bool need_sb, bool need_dsdt, bool need_old, bool need_new);
+size_t rhs_box_scratch_doubles(const int n[3]);
+struct RhsBox;
+RhsBox layout_rhs_box(const mfg_box& b, const mfg_geom& g, double* base);
+bool weno_fast_mode();
+
 cudaError_t upload_params(const DevParams& h);
 cudaError_t read_status(unsigned* v, bool clear);
 cudaError_t launch_rhs_box(const RhsBox& B, int stage, double dt, bool fast, cudaStream_t st);

@@ -40,7 +40,7 @@ __device__ __forceinline__ double thermo_t(double rho, double pres, const double
 template <int NS>
 __device__ __forceinline__ double thermo_p(double rhoe, double rho, const double* spec) {
     const DevParams& P = c_P;
-    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return rhoe * (P.gamma_single - 1.0);
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return rhoe * P.gm1_single;
     if (P.thermo_kind == MFG_THERMO_BG_GAS) {
         double sum_ciMi = 0.0;
 #pragma unroll

@@ -131,7 +131,7 @@ __device__ __forceinline__ double split_pres_m(double M, double alpha) {
 __device__ __forceinline__ void muscl(double uim2, double uL, double uR, double uip1, double& uLh, double& uRh) {
     double delt1 = uip1 - uR;
     double delt2 = uL - uim2;
-    double q = fabs((delt1 - delt2) / ((fabs(delt1) + fabs(delt2)) + kTiny));
+    double q = fabs((delt1 - delt2) * rcp_pos((fabs(delt1) + fabs(delt2)) + kTiny));
     double psi = 1.0 - q * q;
     double L = (0.5 * psi) * (delt1 + delt2);
     uLh = uL + 0.5 * L;
@@ -203,14 +203,14 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
 
     bool fallback = false;
 #pragma unroll
-    for (int q = -3; q <= 2; ++q) fallback |= (vf[oR + q * sd] < 1.0);
+    for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
     const double facevfrac = 0.5 * (vf[oL] + vf[oR]);
     const bool active = P.do_ns && (facevfrac >= 0.5);
 
     double fs[NFS];
 #pragma unroll
     for (int q = 0; q < NFS; ++q) fs[q] = 0.0;
-    fs[FS_FLAGS] = (double)((active ? 1 : 0) | ((P.do_ns && fallback) ? 2 : 0));
+    fs[FS_FLAGS] = __longlong_as_double((active ? 1 : 0) | ((P.do_ns && fallback) ? 2 : 0));  // bit pattern
     double uL[NCONS + NS], uR[NCONS + NS];  // AUSM+-up face states (orders 1, 2)
 
     if (active) {
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
                 }
             }
             const double rL = uL[RHO], rR = uR[RHO];
-            const double irL = 1.0 / rL, irR = 1.0 / rR;
+            const double irL = rcp_pos(rL), irR = rcp_pos(rR);
             const double vxL = uL[RHOU] * irL, vyL = uL[RHOV] * irL, vzL = uL[RHOW] * irL;
             const double vxR = uR[RHOU] * irR, vyR = uR[RHOV] * irR, vzR = uR[RHOW] * irR;
             const double kL = (vxL * vxL + vyL * vyL) + vzL * vzL;
@@ -268,17 +268,17 @@ __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
             const double HR = (cg ? P.g_gm1 : gR / (gR - 1.0)) * (pR * irR) + 0.5 * kR;
             const double rho_half = 0.5 * (rL + rR);
             double as2 = (cg ? P.astar_fac : (2.0 * (gL - 1.0)) / (gL + 1.0)) * HL;
-            const double ahL = as2 / fmax(sqrt(as2), fabs(vL));
+            const double ahL = as2 * rcp_pos(fmax(sqrt(as2), fabs(vL)));
             as2 = (cg ? P.astar_fac : (2.0 * (gR - 1.0)) / (gR + 1.0)) * HR;
-            const double ahR = as2 / fmax(sqrt(as2), fabs(vR));
+            const double ahR = as2 * rcp_pos(fmax(sqrt(as2), fabs(vR)));
             const double ah = fmin(ahL, ahR);
-            const double iah = 1.0 / ah;
+            const double iah = rcp_pos(ah);
             const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
             const double Mb2 = (0.5 * (vL * vL + vR * vR)) * (iah * iah);
             const double Mo = sqrt(fmin(1.0, fmax(Mb2, 0.3 * 0.3)));
             const double fa = Mo * (2.0 - Mo);
-            Mh = Mh - (((0.25 / fa) * fmax(1.0 - Mb2, 0.0)) * (pR - pL)) * ((iah * iah) / rho_half);
+            Mh = Mh - ((fmax(1.0 - Mb2, 0.0) * (pR - pL)) * (iah * iah)) * (0.25 * rcp_pos(fa * rho_half));
             double modM = fabs(Mh);
             if (modM <= 0.3) modM = (Mh * Mh + 0.3 * 0.3) / (2.0 * 0.3);
             const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(TPB) flux_kernel(RhsBox B, int d) {
     const int64_t oL = oR - sd;
     const Fab& FS = B.fs[d];
     const int64_t qf = FS.off(f.i, f.j, f.k);
-    const int flags = (int)FS.p[qf + FS_FLAGS * FS.ns];
+    const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
     const bool active = flags & 1, fallback = flags & 2;
     const double* u = S.p + sc * S.ns;
 
