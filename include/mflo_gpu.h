@@ -67,6 +67,10 @@ extern "C" {
 #define MFG_ERR_TIMEOUT       5   /* a bounded device wait gave up */
 #define MFG_ERR_CUDA          6   /* a CUDA runtime call failed */
 #define MFG_ERR_STATE         7   /* called before mfg_init / unsupported configuration */
+#define MFG_ERR_SIZE          8   /* a box needs more scratch than mfg_compute_dsdt_flow_noalloc's static array */
+
+/* capacity of the static scratch array of mfg_compute_dsdt_flow_noalloc (32 MiB) */
+#define MFG_NOALLOC_SCRATCH_DOUBLES 4194304
 
 /* sticky device status bits (mfg_status) */
 #define MFG_STATUS_NAN           0x1u
@@ -282,6 +286,20 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom,
  * division per reconstructed value (default), 0 follows the reference's
  * four reciprocals (flux_schemes.H:407-414) operation for operation. */
 int mfg_set_weno_mode(int fast);
+
+/* Same result as mfg_compute_dsdt_flow, for callers that may not allocate
+ * device memory (for example an AMReX application, whose arena reserves most
+ * of the GPU at start-up, or a code with a fixed device-memory budget): the
+ * scratch comes from one static device array of MFG_NOALLOC_SCRATCH_DOUBLES
+ * doubles inside the library, and the call makes no cudaMalloc or cudaFree.
+ * A box whose scratch exceeds the array returns MFG_ERR_SIZE (any 32^3 box
+ * fits, for every species count; a 40^3 box does not).  All calls share the array: calls that overlap on
+ * the GPU race.  The first call on each device looks up the array's device
+ * address; make it before any stream capture.  No counterpart in the
+ * reference, which allocates its flux and transport FABs per box
+ * (Source/mflo_evolve.cpp:566-591). */
+int mfg_compute_dsdt_flow_noalloc(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                                  double time, double dt, void* stream);
 
 /* ---- diagnostics (no counterpart in the reference beyond BL_PROFILE) ------ */
 

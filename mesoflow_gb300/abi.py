@@ -15,7 +15,8 @@ NGROW = 3
 RHO, RHOU, RHOV, RHOW, RHOE = 0, 1, 2, 3, 4
 DENS, VELX, VELY, VELZ, PRES, TEMP, VFRAC = 5, 6, 7, 8, 9, 10, 11
 
-OK, ERR_ARG, ERR_NAN, ERR_NEG_PRESSURE, ERR_SCHEME, ERR_TIMEOUT, ERR_CUDA, ERR_STATE = range(8)
+OK, ERR_ARG, ERR_NAN, ERR_NEG_PRESSURE, ERR_SCHEME, ERR_TIMEOUT, ERR_CUDA, ERR_STATE, ERR_SIZE = range(9)
+NOALLOC_SCRATCH_DOUBLES = 4194304
 STATUS_NAN, STATUS_NEG_PRESSURE, STATUS_TIMEOUT, STATUS_BAD_BOX = 0x1, 0x2, 0x4, 0x8
 
 THERMO_MOLAR, THERMO_MASS_SINGLE, THERMO_BG_GAS = 0, 1, 2
@@ -28,6 +29,7 @@ ERROR_NAMES = {
     OK: "ok", ERR_ARG: "bad argument", ERR_NAN: "NaN detected in dsdt",
     ERR_NEG_PRESSURE: "Pressure has gone negative", ERR_SCHEME: "unknown hyperbolics scheme",
     ERR_TIMEOUT: "device wait timed out", ERR_CUDA: "CUDA error", ERR_STATE: "library not initialised",
+    ERR_SIZE: "box needs more scratch than the static array of the allocation-free entry point",
 }
 
 
@@ -101,6 +103,7 @@ SIGNATURES = [
     ("mfg_profile_read", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
     ("mfg_profile_name", C.c_char_p, [C.c_int]),
     ("mfg_launch_count", C.c_ulonglong, []),
+    ("mfg_compute_dsdt_flow_noalloc", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, _VP]),
 ]
 
 _lib = None
