@@ -317,6 +317,11 @@ const char* mfg_profile_name(int kind);
 /* Total kernel launches issued by the library since it was loaded. */
 unsigned long long mfg_launch_count(void);
 
+/* Measures this GPU's FP64 FMA issue rate (TFLOP/s, FMA = 2 flop) with a
+ * register-resident DFMA loop timed by CUDA events; the roof of the RHS
+ * kernels.  Allocates a small buffer.  Synchronizes. */
+int mfg_measure_fp64_peak(double* tflops, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

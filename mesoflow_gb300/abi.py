@@ -104,6 +104,7 @@ SIGNATURES = [
     ("mfg_profile_name", C.c_char_p, [C.c_int]),
     ("mfg_launch_count", C.c_ulonglong, []),
     ("mfg_compute_dsdt_flow_noalloc", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, _VP]),
+    ("mfg_measure_fp64_peak", C.c_int, [C.POINTER(C.c_double), _VP]),
 ]
 
 _lib = None

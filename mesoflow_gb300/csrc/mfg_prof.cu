@@ -95,3 +95,52 @@ const char* mfg_profile_name(int kind) { return (kind >= 0 && kind < K_COUNT) ? 
 unsigned long long mfg_launch_count(void) { return g_launches; }
 
 }  // extern "C"
+
+// ---- FP64 issue-rate probe (the roof of every hot kernel here) ------------
+namespace mfg {
+namespace {
+__global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = threadIdx.x * 1e-3 + q;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += x[q];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+}  // namespace mfg
+
+extern "C" int mfg_measure_fp64_peak(double* tflops, void* stream) {
+    if (!tflops) return MFG_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MFG_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* buf = nullptr;
+    if (cudaMalloc(&buf, sizeof(double) * blocks * threads) != cudaSuccess) return MFG_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0, st);
+        dfma_probe_kernel<<<blocks, threads, 0, st>>>(buf, iters, 0.9999999, 1e-7);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    const double flop = 2.0 * 8.0 * iters * (double)blocks * threads;
+    *tflops = flop / (best * 1e-3) / 1e12;
+    return cudaGetLastError() == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
