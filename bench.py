@@ -31,7 +31,6 @@ sys.path.insert(0, ROOT)
 METRIC = "RK3 cell-updates/s (FP64 256^3 IB)"
 UNIT = "cell-updates/s"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-FP64_PEAK_TFLOPS = 1.256  # measured DFMA issue rate: 2 DFMA/clk/SM x 152 SMs x 2.07 GHz x 2 flop
 
 
 def workload_args(a):
@@ -277,17 +276,27 @@ def main():
     peaks, src = read_peaks()
     abytes = algorithmic(dom, case, a, kernels[dom]["launches"])
     achieved = abytes / (avg_ms / 1e3) / 1e9
-    prof_path = os.path.join(ROOT, "profiles", "flux_traffic.json")
-    traffic = None
-    if os.path.exists(prof_path):
-        with open(prof_path) as f:
-            tr = json.load(f)
-        if tr.get("kernel") == dom and tr.get("order") == a.order:
-            traffic = tr.get("dram_bytes_per_launch_scaled")
+    # per-launch DRAM traffic and FP64 flop of the dominant kernel from the committed ncu capture
+    counts = {}
+    cpath = os.path.join(ROOT, "profiles", "kernel_counts.json")
+    if os.path.exists(cpath):
+        with open(cpath) as f:
+            counts = json.load(f).get(dom, {})
+    traffic = counts.get("dram_bytes_per_launch") if counts.get("order_hyp") == a.order else None
+    fp64_peak = C.c_double()
+    abi.check("mfg_measure_fp64_peak", lib.mfg_measure_fp64_peak(C.byref(fp64_peak), st))
+    flop = counts.get("fp64_flop_per_launch") if counts.get("order_hyp") == a.order else None
+    fp64 = None
+    if flop:
+        ach = flop / (avg_ms / 1e3) / 1e12
+        fp64 = {"achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s", "frac": ach / fp64_peak.value,
+                "flop_per_launch": flop, "flop_source": "profiles/kernel_counts.json (ncu)",
+                "peak_source": "measured live: mfg_measure_fp64_peak (DFMA loop, FMA = 2 flop)"}
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
             "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic, "peak_source": src,
             "algorithmic_bytes_per_launch": abytes, "avg_launch_ms": avg_ms,
-            "share_of_step": kernels[dom]["ms"] / tot if tot else None}
+            "share_of_step": kernels[dom]["ms"] / tot if tot else None, "fp64": fp64,
+            "binding_roof": "fp64 issue (the stencil needs ~10^3 FP64 ops per cell per RHS against ~64 N bytes per cell-update)"}
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
            "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -298,7 +307,9 @@ def main():
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
            "gpu_launches": launches, "clocks": clk, "roofline": roof,
            "kernels_ms_per_step": {k: v["ms"] for k, v in kernels.items()},
-           "fp64_peak_tflops": FP64_PEAK_TFLOPS}
+           "fp64_peak_tflops_live": fp64_peak.value,
+           "algorithmic_bytes_per_cell_update": 64 * case.ncomp,
+           "step_hbm_roofline_frac": value / world * 64 * case.ncomp / (peaks.get("hbm_gbs") * 1e9)}
     if rank == 0 and not a.no_cpu:
         v, th, sample = cpu_port_time(a)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample}

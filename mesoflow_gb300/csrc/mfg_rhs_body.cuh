@@ -1,0 +1,554 @@
+// Per-item bodies of the flow right-hand side (prim / face / flux / update),
+// shared by the per-box launches (mfg_rhs.cu) and the batched persistent
+// launches over all boxes of all levels (mfg_batch.cu).  See mfg_rhs.cu for
+// the structure and the reference semantics.
+#pragma once
+#include "mfg_internal.h"
+#include "mfg_physics.cuh"
+
+namespace mfg {
+namespace {
+
+constexpr double kEpsWeno = 1e-6;
+
+// ---------------------------------------------------------------------------
+// index helpers
+// ---------------------------------------------------------------------------
+struct Idx3 {
+    int i, j, k;
+};
+
+__device__ __forceinline__ Idx3 delinear(int64_t t, const int lo[3], const int len[3]) {
+    int64_t a = t / len[0];
+    Idx3 r;
+    r.i = lo[0] + (int)(t - a * len[0]);
+    r.k = lo[2] + (int)(a / len[1]);
+    r.j = lo[1] + (int)(a - (int64_t)(r.k - lo[2]) * len[1]);
+    return r;
+}
+
+// Euler flux of component c along d at one cell (consprim_funcs.H:48-81 with
+// a unit normal e_d: the products with the zero normal components are exact
+// zeros and drop out).  Rounding-faithful helpers keep the reference's
+// separate multiply and add.
+__device__ __forceinline__ double euler_flux(int c, int d, double u_c, double rho, double va, double vd,
+                                             double p, double E) {
+    if (c == RHO) return mul(rho, vd);
+    if (c <= RHOW) {
+        double t = mul(mul(rho, va), vd);
+        return (c - 1 == d) ? add(t, p) : t;
+    }
+    if (c == RHOE) return mul(add(E, p), vd);
+    return mul(u_c, vd);
+}
+
+// One WENO5-JS edge value (flux_schemes.H:373-446).  Inputs are the five
+// stencil values ordered from the far upwind cell (a) to the far downwind
+// cell (e); the right-biased edge passes them mirrored.  MIR selects the
+// operand order of the reference's third candidate polynomial for the mirrored
+// call.  FAST normalises the three nonlinear weights with one division
+// (w_k/(eps+b_k)^2 / sum = w_k e_k / sum w_j e_j, e_k = prod_{j!=k} (eps+b_j)^2)
+// instead of four; the result differs from the reference by a few ulp.
+template <bool MIR, bool FAST>
+__device__ __forceinline__ double weno_edge(double a, double b, double c, double d, double e) {
+    double t = (a - 2.0 * b) + c;
+    double t2 = (a - 4.0 * b) + 3.0 * c;
+    double b2 = (13.0 / 12.0) * (t * t) + 0.25 * (t2 * t2);
+    t = (b - 2.0 * c) + d;
+    double b1 = (13.0 / 12.0) * (t * t) + (0.25 * (b - d)) * (b - d);
+    t = (c - 2.0 * d) + e;
+    t2 = (3.0 * c - 4.0 * d) + e;
+    double b0 = (13.0 / 12.0) * (t * t) + 0.25 * (t2 * t2);
+    double v2 = MIR ? (11.0 * c - 7.0 * b) + 2.0 * a : (2.0 * a - 7.0 * b) + 11.0 * c;
+    double v1 = (-b + 5.0 * c) + 2.0 * d;
+    double v0 = (2.0 * c + 5.0 * d) - e;
+    if (FAST) {
+        double d2 = (kEpsWeno + b2) * (kEpsWeno + b2);
+        double d1 = (kEpsWeno + b1) * (kEpsWeno + b1);
+        double d0 = (kEpsWeno + b0) * (kEpsWeno + b0);
+        double e2 = d1 * d0, e1 = 6.0 * (d2 * d0), e0 = 3.0 * (d2 * d1);
+        double num = (e2 * v2 + e1 * v1) + e0 * v0;
+        double den = (e2 + e1) + e0;
+        return num / (6.0 * den);
+    }
+    double a2 = 1.0 / ((kEpsWeno + b2) * (kEpsWeno + b2));
+    double a1 = 6.0 * (1.0 / ((kEpsWeno + b1) * (kEpsWeno + b1)));
+    double a0 = 3.0 * (1.0 / ((kEpsWeno + b0) * (kEpsWeno + b0)));
+    double inv = 1.0 / ((a2 + a1) + a0);
+    return ((1.0 / 6.0) * inv) * ((a2 * v2 + a1 * v1) + a0 * v0);
+}
+
+// Face value pair of the stencil s[0..5] = cells i-3 .. i+2 of face i:
+// up = left-biased value (cells i-3..i+1), um = right-biased (cells i-2..i+2).
+template <bool FAST>
+__device__ __forceinline__ void weno_face(const double s[6], double& up, double& um) {
+    up = weno_edge<false, FAST>(s[0], s[1], s[2], s[3], s[4]);
+    um = weno_edge<true, FAST>(s[5], s[4], s[3], s[2], s[1]);
+}
+
+// AUSM+-up split functions (flux_schemes.H:107-181), beta = 1/8.
+__device__ __forceinline__ double split_mach_p(double M) {
+    return (fabs(M) <= 1.0) ? (0.25 * (M + 1.0)) * (M + 1.0) + (0.125 * (M * M - 1.0)) * (M * M - 1.0)
+                            : 0.5 * (M + fabs(M));
+}
+__device__ __forceinline__ double split_mach_m(double M) {
+    return (fabs(M) <= 1.0) ? (-0.25 * (M - 1.0)) * (M - 1.0) - (0.125 * (M * M - 1.0)) * (M * M - 1.0)
+                            : 0.5 * (M - fabs(M));
+}
+__device__ __forceinline__ double split_pres_p(double M, double alpha) {
+    return (fabs(M) <= 1.0) ? ((0.25 * (M + 1.0)) * (M + 1.0)) * (2.0 - M) + ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
+                            : (0.5 * (M + fabs(M))) / M;
+}
+__device__ __forceinline__ double split_pres_m(double M, double alpha) {
+    return (fabs(M) <= 1.0) ? ((0.25 * (M - 1.0)) * (M - 1.0)) * (2.0 + M) - ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
+                            : (0.5 * (M - fabs(M))) / M;
+}
+
+// MUSCL state of component c with the Tatsumi-Martinelli-Jameson limiter
+// (compute_flux_3d.H:33-65): returns uL + L/2 and uR - L/2.
+__device__ __forceinline__ void muscl(double uim2, double uL, double uR, double uip1, double& uLh, double& uRh) {
+    double delt1 = uip1 - uR;
+    double delt2 = uL - uim2;
+    double q = fabs((delt1 - delt2) * rcp_pos((fabs(delt1) + fabs(delt2)) + kTiny));
+    double psi = 1.0 - q * q;
+    double L = (0.5 * psi) * (delt1 + delt2);
+    uLh = uL + 0.5 * L;
+    uRh = uR - 0.5 * L;
+}
+
+// ---------------------------------------------------------------------------
+// prim_kernel: per-cell scalars over grow(bx, 3)
+// ---------------------------------------------------------------------------
+template <int NS>
+__device__ __forceinline__ void prim_body(const RhsBox& B, int64_t t) {
+    int lo[3], len[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = B.lo[d] - MFG_NGROW;
+        len[d] = B.hi[d] - B.lo[d] + 1 + 2 * MFG_NGROW;
+    }
+    const int64_t n = (int64_t)len[0] * len[1] * len[2];
+    if (t >= n) return;
+    const Idx3 c = delinear(t, lo, len);
+    const Fab& S = B.sb;
+    const int64_t o = S.off(c.i, c.j, c.k);
+    const double rho = S.p[o + RHO * S.ns];
+    const double m0 = S.p[o + RHOU * S.ns], m1 = S.p[o + RHOV * S.ns], m2 = S.p[o + RHOW * S.ns];
+    const double E = S.p[o + RHOE * S.ns];
+    double spec[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) spec[s] = (s < c_P.nspec) ? S.p[o + (NFLO + s) * S.ns] : 0.0;
+    // cons_to_prim (consprim_funcs.H:9-23)
+    const double vx = m0 / rho, vy = m1 / rho, vz = m2 / rho;
+    const double rhoe = E - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
+    const double pf = thermo_p<NS>(rhoe, rho, spec);
+    // get_max_eigenvalue's own-species terms (flux_schemes.H:21-43)
+    const double reig = E - (0.5 * ((m0 * m0 + m1 * m1) + m2 * m2)) / rho;
+    const double peig = thermo_p<NS>(reig, rho, spec);
+    const double gam = thermo_gamma<NS>(rho, spec);
+    const double aown = sqrt((gam * peig) / rho);
+    const Fab& X = B.aux;
+    const int64_t q = X.off(c.i, c.j, c.k);
+    X.p[q + AUX_VX * X.ns] = vx;
+    X.p[q + AUX_VY * X.ns] = vy;
+    X.p[q + AUX_VZ * X.ns] = vz;
+    X.p[q + AUX_PF * X.ns] = pf;
+    X.p[q + AUX_REIG * X.ns] = reig;
+    X.p[q + AUX_AOWN * X.ns] = aown;
+    X.p[q + AUX_GAM * X.ns] = gam;
+}
+
+// ---------------------------------------------------------------------------
+// face_kernel: per-face scalars for direction d
+// ---------------------------------------------------------------------------
+template <int NS>
+__device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    const int64_t nf = (int64_t)len[0] * len[1] * len[2];
+    if (t >= nf) return;
+    const Idx3 f = delinear(t, lo, len);
+    const DevParams& P = c_P;
+    const Fab& S = B.sb;
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+    const int64_t st1 = (t1 == 0) ? 1 : (t1 == 1) ? S.js : S.ks;
+    const int64_t st2 = (t2 == 0) ? 1 : (t2 == 1) ? S.js : S.ks;
+    const int64_t oR = S.off(f.i, f.j, f.k);  // right cell: face i separates i-1 and i
+    const int64_t oL = oR - sd;
+    const double* vf = S.p + VFRAC * S.ns;
+
+    bool fallback = false;
+#pragma unroll
+    for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
+    const double facevfrac = 0.5 * (vf[oL] + vf[oR]);
+    const bool active = P.do_ns && (facevfrac >= 0.5);
+
+    double fs[NFS];
+#pragma unroll
+    for (int q = 0; q < NFS; ++q) fs[q] = 0.0;
+    fs[FS_FLAGS] = __longlong_as_double((active ? 1 : 0) | ((P.do_ns && fallback) ? 2 : 0));  // bit pattern
+    double uL[NCONS + NS], uR[NCONS + NS];  // AUSM+-up face states (orders 1, 2)
+
+    if (active) {
+        const int ord = P.order_hyp;
+        if (ord == 5 || ord == 4) {
+            const Fab& X = B.aux;
+            const int64_t qL = X.off(f.i, f.j, f.k) - ((d == 0) ? 1 : (d == 1) ? X.js : X.ks);
+            const int64_t qR = X.off(f.i, f.j, f.k);
+            const double* vd = X.p + (AUX_VX + d) * X.ns;
+            const double veln = fmax(fabs(vd[qL]), fabs(vd[qR]));
+            const double aL = X.p[qL + AUX_AOWN * X.ns];
+            double aR;
+            if (ord == 5) {
+                // presR is evaluated with the left cell's species (flux_schemes.H:33)
+                double specL[NS];
+#pragma unroll
+                for (int s = 0; s < NS; ++s) specL[s] = (s < P.nspec) ? S.p[oL + (NFLO + s) * S.ns] : 0.0;
+                const double rhoR = S.p[oR + RHO * S.ns];
+                const double pR = thermo_p<NS>(X.p[qR + AUX_REIG * X.ns], rhoR, specL);
+                aR = sqrt((X.p[qR + AUX_GAM * X.ns] * pR) / rhoR);
+            } else {
+                aR = X.p[qR + AUX_AOWN * X.ns];
+            }
+            fs[FS_LAMBDA] = fmax(aL, aR) + veln;
+        } else {
+            // AUSM+-up (flux_schemes.H:185-310) on first- or second-order states
+            const int nc = NCONS + P.nspec;
+#pragma unroll
+            for (int c = 0; c < NCONS + NS; ++c) {
+                if (c >= nc) { uL[c] = uR[c] = 0.0; continue; }
+                const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+                double ul = S.p[oL + sc * S.ns], ur = S.p[oR + sc * S.ns];
+                if (ord == 2) {
+                    double ulm1 = fallback ? ul : S.p[oL - sd + sc * S.ns];
+                    double urp1 = fallback ? ur : S.p[oR + sd + sc * S.ns];
+                    muscl(ulm1, ul, ur, urp1, uL[c], uR[c]);
+                } else {
+                    uL[c] = ul;
+                    uR[c] = ur;
+                }
+            }
+            const double rL = uL[RHO], rR = uR[RHO];
+            const double irL = rcp_pos(rL), irR = rcp_pos(rR);
+            const double vxL = uL[RHOU] * irL, vyL = uL[RHOV] * irL, vzL = uL[RHOW] * irL;
+            const double vxR = uR[RHOU] * irR, vyR = uR[RHOV] * irR, vzR = uR[RHOW] * irR;
+            const double kL = (vxL * vxL + vyL * vyL) + vzL * vzL;
+            const double kR = (vxR * vxR + vyR * vyR) + vzR * vzR;
+            const double pL = thermo_p<NS>(uL[RHOE] - (0.5 * rL) * kL, rL, uL + NCONS);
+            const double pR = thermo_p<NS>(uR[RHOE] - (0.5 * rR) * kR, rR, uR + NCONS);
+            const double gL = thermo_gamma<NS>(rL, uL + NCONS), gR = thermo_gamma<NS>(rR, uR + NCONS);
+            const double vL = (d == 0) ? vxL : (d == 1) ? vyL : vzL;
+            const double vR = (d == 0) ? vxR : (d == 1) ? vyR : vzR;
+            const bool cg = P.thermo_kind == MFG_THERMO_MASS_SINGLE;
+            const double HL = (cg ? P.g_gm1 : gL / (gL - 1.0)) * (pL * irL) + 0.5 * kL;
+            const double HR = (cg ? P.g_gm1 : gR / (gR - 1.0)) * (pR * irR) + 0.5 * kR;
+            const double rho_half = 0.5 * (rL + rR);
+            double as2 = (cg ? P.astar_fac : (2.0 * (gL - 1.0)) / (gL + 1.0)) * HL;
+            const double ahL = as2 * rcp_pos(fmax(sqrt(as2), fabs(vL)));
+            as2 = (cg ? P.astar_fac : (2.0 * (gR - 1.0)) / (gR + 1.0)) * HR;
+            const double ahR = as2 * rcp_pos(fmax(sqrt(as2), fabs(vR)));
+            const double ah = fmin(ahL, ahR);
+            const double iah = rcp_pos(ah);
+            const double ML = vL * iah, MR = vR * iah;
+            double Mh = split_mach_p(ML) + split_mach_m(MR);
+            const double Mb2 = (0.5 * (vL * vL + vR * vR)) * (iah * iah);
+            const double Mo = sqrt(fmin(1.0, fmax(Mb2, 0.3 * 0.3)));
+            const double fa = Mo * (2.0 - Mo);
+            Mh = Mh - ((fmax(1.0 - Mb2, 0.0) * (pR - pL)) * (iah * iah)) * (0.25 * rcp_pos(fa * rho_half));
+            double modM = fabs(Mh);
+            if (modM <= 0.3) modM = (Mh * Mh + 0.3 * 0.3) / (2.0 * 0.3);
+            const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
+            const double PLp = split_pres_p(ML, alpha), PRm = split_pres_m(MR, alpha);
+            double ph = PLp * pL + PRm * pR;
+            ph = ph - ((((0.75 * PLp) * PRm) * (rL + rR)) * (fa * ah)) * (vR - vL);
+            fs[FS_LAMBDA] = ah;
+            fs[FS_MH] = Mh;
+            fs[FS_MODM] = modM;
+            fs[FS_PH] = ph;
+            fs[FS_PL] = pL;
+            fs[FS_PR] = pR;
+        }
+        // viscous stress (compute_flux_3d.H:293-367); lagged primitive velocities
+        const double* V0 = S.p + VELX * S.ns;
+        const double* V1 = S.p + VELY * S.ns;
+        const double* V2 = S.p + VELZ * S.ns;
+        const double ids = B.idx[d], ih1 = 0.5 * B.idx[t1], ih2 = 0.5 * B.idx[t2];
+        double g[3][3];  // g[component][0: normal, 1: trans1, 2: trans2]
+        const double* Vc[3] = {V0, V1, V2};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double* V = Vc[a];
+            g[a][0] = (V[oR] - V[oL]) * ids;
+            g[a][1] = (0.5 * (V[oL + st1] + V[oR + st1]) - 0.5 * (V[oL - st1] + V[oR - st1])) * ih1;
+            g[a][2] = (0.5 * (V[oL + st2] + V[oR + st2]) - 0.5 * (V[oL - st2] + V[oR - st2])) * ih2;
+        }
+        // gradient along Cartesian axis x/y/z is the entry whose sweep role maps to it
+        const int gx = (d == 0) ? 0 : (d == 1) ? 2 : 1;
+        const int gy = (d == 0) ? 1 : (d == 1) ? 0 : 2;
+        const int gz = (d == 0) ? 2 : (d == 1) ? 1 : 0;
+        const double dudx = g[0][gx], dudy = g[0][gy], dudz = g[0][gz];
+        const double dvdx = g[1][gx], dvdy = g[1][gy], dvdz = g[1][gz];
+        const double dwdx = g[2][gx], dwdy = g[2][gy], dwdz = g[2][gz];
+        // viscosity always from cells (i,j,k) and (i-1,j,k) (compute_flux_3d.H:179)
+        const double mu = (P.visc_mode == MFG_TRANSPORT_CONST)
+                              ? P.visc_hm
+                              : harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR]),
+                                              blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR - 1]));
+        const double delu = (dudx + dvdy) + dwdz;
+        double tau[3][3];
+        tau[0][0] = mu * (2.0 * dudx - kTwo3rd * delu);
+        tau[0][1] = mu * (dudy + dvdx);
+        tau[0][2] = mu * (dudz + dwdx);
+        tau[1][0] = mu * (dvdx + dudy);
+        tau[1][1] = mu * (2.0 * dvdy - kTwo3rd * delu);
+        tau[1][2] = mu * (dvdz + dwdy);
+        tau[2][0] = mu * (dwdx + dudz);
+        tau[2][1] = mu * (dwdy + dvdz);
+        tau[2][2] = mu * (2.0 * dwdz - kTwo3rd * delu);
+        const double fvel[3] = {0.5 * (V0[oL] + V0[oR]), 0.5 * (V1[oL] + V1[oR]), 0.5 * (V2[oL] + V2[oR])};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double tn = tau[d][a];  // tau_{ja} n_j with n = e_d
+            fs[FS_VIS + a] = tn;
+            fs[FS_VISE + a] = tn * fvel[a];
+        }
+    }
+    if (P.do_ns) {
+        // heat conduction (compute_flux_3d.H:373-374), conductivity from (i,j,k),(i-1,j,k)
+        const double kc = (P.cond_mode == MFG_TRANSPORT_CONST)
+                              ? P.cond_hm
+                              : harmonic_mean(blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR]),
+                                              blend(P.cond_mode, P.cond_gas, P.cond_solid, vf[oR - 1]));
+        const double* T = S.p + TEMP * S.ns;
+        fs[FS_THERM] = kc * ((T[oR] - T[oL]) * B.idx[d]);
+    }
+    if (P.do_ns && P.order_hyp <= 2) {
+        // AUSM+-up: the face thread holds the face states and the scheme scalars,
+        // so it writes every component's complete flux (no per-component pass).
+        const Fab& O = B.flx[d];
+        const int64_t qo = O.off(f.i, f.j, f.k);
+        const Fab& U = B.uflux[d];
+        const int64_t qu = U.p ? U.off(f.i, f.j, f.k) : 0;
+#pragma unroll
+        for (int c = 0; c < NCONS + NS; ++c) {
+            if (c >= NCONS + P.nspec) break;
+            const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+            double F = 0.0;
+            if (active) {
+                double fL = uL[c], fR = uR[c];
+                if (c == RHOE) {
+                    fL = uL[c] + fs[FS_PL];
+                    fR = uR[c] + fs[FS_PR];
+                }
+                double fh = ((0.5 * fs[FS_MH]) * (fL + fR) - (0.5 * fs[FS_MODM]) * (fR - fL)) * fs[FS_LAMBDA];
+                if (c == 1 + d) fh += fs[FS_PH];
+                F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
+                if (c >= RHOU && c <= RHOW) F -= fs[FS_VIS + c - 1];
+                if (c == RHOE) {
+                    F -= fs[FS_VISE + 0];
+                    F -= fs[FS_VISE + 1];
+                    F -= fs[FS_VISE + 2];
+                }
+            }
+            if (c == RHOE) F -= fs[FS_THERM];
+            if (c >= NCONS) {
+                const int s = c - NCONS;
+                const double Dh = (P.diff_mode[s] == MFG_TRANSPORT_CONST)
+                                      ? P.diff_hm[s]
+                                      : harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oL]),
+                                                      blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oR]));
+                F -= (Dh * (S.p[oR + sc * S.ns] - S.p[oL + sc * S.ns])) * B.idx[d];
+            }
+            O.p[qo + c * O.ns] = F;
+            if (U.p) U.p[qu + sc * U.ns] = F;
+        }
+        if (U.p)
+            for (int z = NCONS; z < NFLO; ++z) U.p[qu + z * U.ns] = 0.0;
+        return;
+    }
+    const Fab& F = B.fs[d];
+    const int64_t q = F.off(f.i, f.j, f.k);
+#pragma unroll
+    for (int c = 0; c < NFS; ++c) F.p[q + c * F.ns] = fs[c];
+}
+
+// ---------------------------------------------------------------------------
+// flux_kernel: per (face, component) along d
+// ---------------------------------------------------------------------------
+template <bool FAST>
+__device__ __forceinline__ void flux_body(const RhsBox& B, int d, int c, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    const int64_t nf = (int64_t)len[0] * len[1] * len[2];
+    if (t >= nf) return;  // c: advected component 0..4, 5.. = species
+    const Idx3 f = delinear(t, lo, len);
+    const DevParams& P = c_P;
+    const Fab& S = B.sb;
+    const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);  // state component
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int64_t oR = S.off(f.i, f.j, f.k);
+    const int64_t oL = oR - sd;
+    const Fab& FS = B.fs[d];
+    const int64_t qf = FS.off(f.i, f.j, f.k);
+    const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
+    const bool active = flags & 1, fallback = flags & 2;
+    const double* u = S.p + sc * S.ns;
+
+    double F = 0.0;
+    if (P.do_ns) {
+        if (active) {
+            const int ord = P.order_hyp;
+            double fh;
+            if (ord == 5 || ord == 4) {
+                const Fab& X = B.aux;
+                const int64_t xd = (d == 0) ? 1 : (d == 1) ? X.js : X.ks;
+                const int64_t xR = X.off(f.i, f.j, f.k);
+                const double lam = FS.p[qf + FS_LAMBDA * FS.ns];
+                double us[6], fl[6];
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    int qq = q - 3;
+                    if (fallback) qq = (q < 3) ? -1 : 0;  // first-order stencil (:233-249)
+                    const int64_t os = oR + qq * sd, ox = xR + qq * xd;
+                    us[q] = u[os];
+                    const double rho = S.p[os + RHO * S.ns];
+                    const double vd = X.p[ox + (AUX_VX + d) * X.ns];
+                    const double va = (c >= 1 && c <= 3) ? X.p[ox + (AUX_VX + c - 1) * X.ns] : 0.0;
+                    const double p = X.p[ox + AUX_PF * X.ns];
+                    const double E = S.p[os + RHOE * S.ns];
+                    fl[q] = euler_flux(c, d, us[q], rho, va, vd, p, E);
+                }
+                if (ord == 5) {
+                    double fp, fm, up, um;
+                    weno_face<FAST>(fl, fp, fm);
+                    weno_face<FAST>(us, up, um);
+                    fh = 0.5 * (fp + lam * up) + 0.5 * (fm - lam * um);
+                } else {
+                    // central_with_diss_flux(ul, ur, ulm1, urp1): uim1=ul, ui=ur, uim2=ulm1, uip1=urp1
+                    fh = kTwelveth * (((7.0 * fl[3] + 7.0 * fl[2]) - fl[1]) - fl[4]);
+                    fh -= ((kTwelveth * (((3.0 * us[3] - 3.0 * us[2]) - us[4]) + us[3])) * lam) * P.dissfactor;
+                }
+            } else {
+                double ul = u[oL], ur = u[oR], uLh = ul, uRh = ur;
+                if (ord == 2) {
+                    const double ulm1 = fallback ? ul : u[oL - sd];
+                    const double urp1 = fallback ? ur : u[oR + sd];
+                    muscl(ulm1, ul, ur, urp1, uLh, uRh);
+                }
+                const double Mh = FS.p[qf + FS_MH * FS.ns];
+                const double modM = FS.p[qf + FS_MODM * FS.ns];
+                const double ah = FS.p[qf + FS_LAMBDA * FS.ns];
+                double fL = uLh, fR = uRh;
+                if (c == RHOE) {
+                    fL = uLh + FS.p[qf + FS_PL * FS.ns];
+                    fR = uRh + FS.p[qf + FS_PR * FS.ns];
+                }
+                fh = ((0.5 * Mh) * (fL + fR) - (0.5 * modM) * (fR - fL)) * ah;
+                if (c == 1 + d) fh += FS.p[qf + FS_PH * FS.ns];
+            }
+            F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
+            if (c >= RHOU && c <= RHOW) F -= FS.p[qf + (FS_VIS + c - 1) * FS.ns];
+            if (c == RHOE) {
+                F -= FS.p[qf + (FS_VISE + 0) * FS.ns];
+                F -= FS.p[qf + (FS_VISE + 1) * FS.ns];
+                F -= FS.p[qf + (FS_VISE + 2) * FS.ns];
+            }
+        }
+        if (c == RHOE) F -= FS.p[qf + FS_THERM * FS.ns];
+    } else if (c >= NCONS) {
+        // species convection without Navier-Stokes (compute_flux_3d.H:382-421);
+        // the limited states reduce to first order (by-value limiter, :69-83)
+        const double* vfp = S.p + VFRAC * S.ns;
+        const double* Vd = S.p + (VELX + d) * S.ns;
+        double velface = 0.5 * (Vd[oL] + Vd[oR]);
+        if (P.species_in_solid) {
+            const double w = (vfp[oL] < 1.0) ? 0.0 : 1.0;  // both weights test the left cell (:410-411)
+            velface = (w * Vd[oL] + w * Vd[oR]) / ((w + w) + kTiny);
+        }
+        F = P.advect_flag[c - NCONS] *
+            ((0.5 * (velface + fabs(velface))) * u[oL] + (0.5 * (velface - fabs(velface))) * u[oR]);
+    }
+    if (c >= NCONS) {
+        // species diffusion (compute_flux_3d.H:425-428)
+        const int s = c - NCONS;
+        const double* vfp = S.p + VFRAC * S.ns;
+        const double Dh = (P.diff_mode[s] == MFG_TRANSPORT_CONST)
+                              ? P.diff_hm[s]
+                              : harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oL]),
+                                              blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vfp[oR]));
+        F -= (Dh * (u[oR] - u[oL])) * B.idx[d];
+    }
+    const Fab& O = B.flx[d];
+    O.p[O.off(f.i, f.j, f.k) + c * O.ns] = F;
+    if (B.uflux[d].p) {
+        const Fab& U = B.uflux[d];
+        const int64_t qu = U.off(f.i, f.j, f.k);
+        U.p[qu + sc * U.ns] = F;
+        if (c == 0)
+            for (int z = NCONS; z < NFLO; ++z) U.p[qu + z * U.ns] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// update_kernel: per (cell, component): divergence, masking, RK stage
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void update_body(const RhsBox& B, int stage, double dt, int n, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1;
+    const int64_t nc = (int64_t)len[0] * len[1] * len[2];
+    if (t >= nc) return;  // n: state component
+    const Idx3 x = delinear(t, lo, len);
+    const DevParams& P = c_P;
+    double ds = 0.0;
+    const bool advected = (n < NCONS) || (n >= NFLO);
+    if (advected) {
+        const int c = (n < NCONS) ? n : n - (NFLO - NCONS);
+        const Fab &Fx = B.flx[0], &Fy = B.flx[1], &Fz = B.flx[2];
+        const int64_t ox = Fx.off(x.i, x.j, x.k) + c * Fx.ns;
+        const int64_t oy = Fy.off(x.i, x.j, x.k) + c * Fy.ns;
+        const int64_t oz = Fz.off(x.i, x.j, x.k) + c * Fz.ns;
+        ds = ((Fx.p[ox] - Fx.p[ox + 1]) * B.idx[0] + (Fy.p[oy] - Fy.p[oy + Fy.js]) * B.idx[1]) +
+             (Fz.p[oz] - Fz.p[oz + Fz.ks]) * B.idx[2];
+        ds = ds + 0.0;  // + source (compute_fluid_source is zero)
+    }
+    const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
+    const int nnull = (P.species_in_solid == 1) ? NFLO : NFLO + P.nspec;
+    if (n != RHOE) {
+        if (n < nnull && vfrac < 1.0) ds = 0.0;
+    } else if (!P.conj_ht) {
+        if (vfrac < 1.0) ds = 0.0;
+    } else if (vfrac > 0.0 && vfrac < 1.0) {
+        ds = 0.0;
+    }
+    if (ds != ds) raise_status(MFG_STATUS_NAN);
+    if (B.dsdt.p) B.dsdt(x.i, x.j, x.k, n) = ds;
+    if (stage == 1) {
+        B.snew(x.i, x.j, x.k, n) = add(B.sb(x.i, x.j, x.k, n), mul(dt, ds));
+    } else if (stage == 2) {
+        double v = B.snew(x.i, x.j, x.k, n);
+        v = add(v, mul(dt, ds));
+        v = add(v, mul(3.0, B.sold(x.i, x.j, x.k, n)));
+        B.snew(x.i, x.j, x.k, n) = mul(v, 0.25);
+    } else if (stage == 3) {
+        double v = B.snew(x.i, x.j, x.k, n);
+        v = add(v, mul(dt, ds));
+        v = add(B.sold(x.i, x.j, x.k, n), mul(2.0, v));
+        B.snew(x.i, x.j, x.k, n) = mul(v, kThird);
+    }
+}
+
+
+// Work items of each phase for one box.
+__host__ __device__ __forceinline__ int64_t prim_items(const RhsBox& B) {
+    return (int64_t)(B.hi[0] - B.lo[0] + 7) * (B.hi[1] - B.lo[1] + 7) * (B.hi[2] - B.lo[2] + 7);
+}
+__host__ __device__ __forceinline__ int64_t face_items(const RhsBox& B, int d) {
+    return (int64_t)(B.hi[0] - B.lo[0] + 1 + (d == 0)) * (B.hi[1] - B.lo[1] + 1 + (d == 1)) *
+           (B.hi[2] - B.lo[2] + 1 + (d == 2));
+}
+__host__ __device__ __forceinline__ int64_t cell_items(const RhsBox& B) {
+    return (int64_t)(B.hi[0] - B.lo[0] + 1) * (B.hi[1] - B.lo[1] + 1) * (B.hi[2] - B.lo[2] + 1);
+}
+
+}  // namespace
+}  // namespace mfg
