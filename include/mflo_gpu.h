@@ -301,6 +301,37 @@ int mfg_set_weno_mode(int fast);
 int mfg_compute_dsdt_flow_noalloc(const mfg_box* boxes, int nbox, const mfg_geom* geom,
                                   double time, double dt, void* stream);
 
+/* ---- batched AMR form --------------------------------------------------------
+ * All boxes of all levels (uneven sizes; boxes[b].level indexes geoms) uploaded
+ * once into device tables; every phase of the step is one launch over a tile
+ * list spanning all boxes, and the whole step can be replayed from one CUDA
+ * graph.  Levels advance with a common dt (no subcycling); level-L ghost cells
+ * not covered at level L are injected from level L-1.  Replaces the per-box
+ * MFIter loops of Source/mflo_evolve.cpp:509-519 and :579-651 (and the
+ * FillPatch calls :278-302) for a whole hierarchy at once. */
+typedef struct mfg_boxlist mfg_boxlist;
+
+/* Builds the device box tables, per-level owner maps, per-box scratch and tile
+ * lists.  The arrays named by the descriptors must stay valid until destroy. */
+int mfg_boxlist_create(const mfg_box* boxes, int nbox, const mfg_geom* geoms, int nlev,
+                       mfg_boxlist** out);
+int mfg_boxlist_destroy(mfg_boxlist* list);
+
+/* One step of every level (phi_old <- phi_new, three RK3 stages of fill + cut
+ * cells + RHS + stage update, chemistry sub-step, primitive refresh, clipping).
+ * mode 0: plain per-box launches of the same kernels; 1: batched launches over
+ * tile lists; 2: the batched step replayed from a CUDA graph (captured on first
+ * use and when dt changes; needs a non-default stream).  Asynchronous. */
+int mfg_boxlist_step(mfg_boxlist* list, double time, double dt, int mode, void* stream);
+
+/* Chooses tile size and grid size for each batched phase by timing candidates
+ * (CUDA events) on this machine list; results (optional, 15 doubles): per phase
+ * tile items, grid blocks, best ms.  Synchronizes. */
+int mfg_boxlist_autotune(mfg_boxlist* list, double dt, double* results, void* stream);
+
+/* Number of valid cells in the list. */
+long long mfg_boxlist_cells(const mfg_boxlist* list);
+
 /* ---- diagnostics (no counterpart in the reference beyond BL_PROFILE) ------ */
 
 /* Enables (1) or disables (0) CUDA-event timing of every kernel launch and

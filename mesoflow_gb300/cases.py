@@ -375,3 +375,147 @@ def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, bloc
     S = state_from_prim(P, rho, u, zero, zero, np.full(shape, pres), spec, vf)
     L = n * dx
     return Case("catalyst", P, shape, (0, 0, 0), (L, L, L), (0, 0, 0), max_grid, S, {"u_in": u_in})
+
+
+# ---------------------------------------------------------------------------
+# multi-level catalyst hierarchy (batched AMR form)
+# ---------------------------------------------------------------------------
+class Geometry:
+    """Analytic catalyst geometry in physical units: one axis-aligned solid block
+    plus seeded spheres; fluid volume fraction by 8-corner sampling of any cell
+    box at any resolution (as the reference's initdata, Prob.H:39-59)."""
+
+    def __init__(self, L, seed, nspheres=24, block=(0.35, 0.65, 0.3, 0.7, 0.3, 0.7), rmin=0.03, rmax=0.07):
+        rng = np.random.default_rng(seed)
+        self.L = L
+        self.block = np.array(block) * L
+        self.c = rng.uniform(0.15, 0.85, size=(nspheres, 3)) * L
+        self.r = rng.uniform(rmin, rmax, size=nspheres) * L
+
+    def vfrac(self, lo, hi, dx):
+        """vfrac of cells lo..hi (inclusive) on a grid of spacing dx, shape (z, y, x)."""
+        ax = [np.arange(lo[d], hi[d] + 2) * dx for d in range(3)]  # corner coordinates
+        Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        b = self.block
+        solid = (X >= b[0]) & (X <= b[1]) & (Y >= b[2]) & (Y <= b[3]) & (Z >= b[4]) & (Z <= b[5])
+        bl = np.array([lo[d] * dx for d in range(3)])
+        bh = np.array([(hi[d] + 1) * dx for d in range(3)])
+        for c, r in zip(self.c, self.r):
+            if np.any(c + r < bl) or np.any(c - r > bh):
+                continue
+            solid |= (X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2 <= r * r
+        f = (~solid).astype(np.float64)
+        return 0.125 * sum(f[kk:kk + f.shape[0] - 1, jj:jj + f.shape[1] - 1, ii:ii + f.shape[2] - 1]
+                           for kk in (0, 1) for jj in (0, 1) for ii in (0, 1))
+
+
+def _merge_blocks(tag, blk, max_blocks):
+    """Greedy merge of tagged blocks (bool array over block indices (z, y, x))
+    into boxes of at most max_blocks blocks per side; returns block-index boxes."""
+    used = np.zeros_like(tag)
+    out = []
+    nz, ny, nx = tag.shape
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                if not tag[z, y, x] or used[z, y, x]:
+                    continue
+                x1 = x
+                while x1 + 1 < nx and x1 + 1 - x < max_blocks and tag[z, y, x1 + 1] and not used[z, y, x1 + 1]:
+                    x1 += 1
+                y1 = y
+                while (y1 + 1 < ny and y1 + 1 - y < max_blocks and tag[z, y1 + 1, x:x1 + 1].all()
+                       and not used[z, y1 + 1, x:x1 + 1].any()):
+                    y1 += 1
+                z1 = z
+                while (z1 + 1 < nz and z1 + 1 - z < max_blocks and tag[z1 + 1, y:y1 + 1, x:x1 + 1].all()
+                       and not used[z1 + 1, y:y1 + 1, x:x1 + 1].any()):
+                    z1 += 1
+                used[z:z1 + 1, y:y1 + 1, x:x1 + 1] = True
+                out.append(((x * blk, y * blk, z * blk), ((x1 + 1) * blk - 1, (y1 + 1) * blk - 1, (z1 + 1) * blk - 1)))
+    return out
+
+
+class AmrCase:
+    """Levels of boxes (uneven sizes), per-level geometry and per-box initial states."""
+
+    def __init__(self, params, geoms, boxes, states, meta):
+        self.params = params
+        self.geoms = geoms            # list of abi.Geom, one per level
+        self.boxes = boxes            # list of (lo, hi, level)
+        self.states = states          # per box (ncomp, nz, ny, nx)
+        self.meta = meta
+
+    @property
+    def ncomp(self):
+        return abi.FLO_NVARS + self.params.nspec
+
+    def cells(self):
+        return sum(int(np.prod([h[d] - l[d] + 1 for d in range(3)])) for l, h, _ in self.boxes)
+
+
+def catalyst_amr(n0=128, nlev=3, order=5, seed=4, blocking=16, max_grid=64, base_grid=32, u_in=1.0, dx0=1e-5,
+                 nspheres=80, nreact=8):
+    """Catalyst block + spheres on 3 levels (ratio 2, base n0^3): level l+1
+    covers the level-l cells within 2 cells of the immersed surface (cut cells
+    and their neighbours), clustered into blocks of `blocking` cells and merged
+    into uneven boxes of up to max_grid cells per side (a stand-in for AMReX's
+    regrid, which is not vendored).  Chemistry, species and boundaries as
+    catalyst(): 8 gas + 2 site species, 8 Arrhenius surface reactions."""
+    base = catalyst(n=8, order=order, seed=seed, nreact=nreact, u_in=u_in, dx=dx0)  # parameter tables only
+    P = base.params
+    L = n0 * dx0
+    geo = Geometry(L, seed, nspheres=nspheres)
+    geoms, boxes = [], []
+    # level 0: the whole domain in base_grid boxes
+    lev_boxes = [((lo[0], lo[1], lo[2]), (hi[0], hi[1], hi[2])) for lo, hi in
+                 chop((0, 0, 0), (n0 - 1, n0 - 1, n0 - 1), base_grid)]
+    for l in range(nlev):
+        n = n0 * 2 ** l
+        geoms.append(geometry((0, 0, 0), (n - 1,) * 3, (0, 0, 0), (L, L, L), (0, 0, 0)))
+        boxes += [(lo, hi, l) for lo, hi in lev_boxes]
+        if l + 1 == nlev:
+            break
+        dx = L / n
+        # tag cells of this level near the surface, in fine-block units
+        nb = (2 * n) // blocking
+        tag = np.zeros((nb, nb, nb), dtype=bool)
+        inside = np.zeros((nb, nb, nb), dtype=bool)
+        for lo, hi in lev_boxes:
+            vf = geo.vfrac(lo, hi, dx)
+            cut = (vf > 0) & (vf < 1)
+            g = np.zeros_like(cut)
+            for ax in range(3):  # grow the cut band by 2 cells
+                for s in (-2, -1, 1, 2):
+                    g |= np.roll(cut, s, axis=ax)
+            g |= cut
+            zz, yy, xx = np.nonzero(g)
+            fz = ((zz + lo[2]) * 2) // blocking
+            fy = ((yy + lo[1]) * 2) // blocking
+            fx = ((xx + lo[0]) * 2) // blocking
+            tag[fz, fy, fx] = True
+            # fine blocks that lie inside this coarse box (proper nesting)
+            bz0, by0, bx0 = (2 * lo[2]) // blocking, (2 * lo[1]) // blocking, (2 * lo[0]) // blocking
+            bz1, by1, bx1 = (2 * (hi[2] + 1)) // blocking, (2 * (hi[1] + 1)) // blocking, (2 * (hi[0] + 1)) // blocking
+            inside[bz0:bz1, by0:by1, bx0:bx1] = True
+        tag &= inside
+        lev_boxes = _merge_blocks(tag, blocking, max_grid // blocking)
+    # initial states: gas at rest except the inlet velocity in fluid cells, sites in solid cells
+    W = [P.molwt[s] for s in range(P.ngas)]
+    T, pres = 500.0, 1e5
+    x = np.array([0.7, 0.1, 0.05, 0.05, 0.04, 0.03, 0.02, 0.01])
+    cg = x * pres / (RU * T)
+    states = []
+    for lo, hi, l in boxes:
+        dx = L / (n0 * 2 ** l)
+        vf = geo.vfrac(lo, hi, dx)
+        shape = vf.shape
+        spec = [np.full(shape, cg[s]) for s in range(P.ngas)]
+        site = np.where(vf < 1.0, 50.0, 0.0)
+        spec += [site * 0.6, site * 0.4]
+        rho = sum(spec[s] * W[s] for s in range(P.ngas))
+        u = np.where(vf == 1.0, u_in, 0.0)
+        zero = np.zeros(shape)
+        states.append(state_from_prim(P, rho, u, zero, zero, np.full(shape, pres), spec, vf))
+    meta = {"nlev": nlev, "per_level_boxes": [sum(1 for b in boxes if b[2] == l) for l in range(nlev)]}
+    return AmrCase(P, geoms, boxes, states, meta)

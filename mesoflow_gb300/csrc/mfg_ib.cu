@@ -89,7 +89,9 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
     c.S = make_fab(b.sborder);
     c.dxmin = fmin(g.dx[0], fmin(g.dx[1], g.dx[2]));
     c.tcht = tcht_scratch;
-    if (g.dx[0] != g_wdir_dx[0] || g.dx[1] != g_wdir_dx[1] || g.dx[2] != g_wdir_dx[2]) {
+    // the table depends on the cell aspect ratios only (dx / dxmin), the same on every level
+    const double dnk[3] = {g.dx[0] / c.dxmin, g.dx[1] / c.dxmin, g.dx[2] / c.dxmin};
+    if (dnk[0] != g_wdir_dx[0] || dnk[1] != g_wdir_dx[1] || dnk[2] != g_wdir_dx[2]) {
         // Dirichlet weights: 1/((l dx_nd)^2 + (m dy_nd)^2 + (n dz_nd)^2 + 1e-40), centre unused
         double w[SW * SW * SW];
         const double dn[3] = {g.dx[0] / c.dxmin, g.dx[1] / c.dxmin, g.dx[2] / c.dxmin};
@@ -103,7 +105,7 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
         cudaError_t e = cudaMemcpyToSymbolAsync(c_wdir, w, sizeof(w), 0, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return e;
         cudaStreamSynchronize(st);
-        for (int d = 0; d < 3; ++d) g_wdir_dx[d] = g.dx[d];
+        for (int d = 0; d < 3; ++d) g_wdir_dx[d] = dnk[d];
     }
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
     ProfScope ps(K_CUT, st);

@@ -1,158 +1,26 @@
 // Step bookends and chemistry: reaction source, SSP-RK3 chemistry sub-step,
 // primitive refresh, species clipping, residual norms and the CFL estimate.
-#include "mfg_internal.h"
-#include "mfg_physics.cuh"
+#include "mfg_step_body.cuh"
 
 namespace mfg {
 namespace {
 
 constexpr int TPB = 256;
 
-struct Valid {
-    int lo[3], len[3];
-    int64_t n;
-};
-
-inline Valid valid_of(const mfg_box& b) {
-    Valid v;
-    v.n = 1;
-    for (int d = 0; d < 3; ++d) {
-        v.lo[d] = b.lo[d];
-        v.len[d] = b.hi[d] - b.lo[d] + 1;
-        v.n *= v.len[d];
-    }
-    return v;
-}
-
-__device__ __forceinline__ void cell_of(const Valid& v, int64_t t, int& i, int& j, int& k) {
-    int64_t a = t / v.len[0];
-    i = v.lo[0] + (int)(t - a * v.len[0]);
-    k = v.lo[2] + (int)(a / v.len[1]);
-    j = v.lo[1] + (int)(a - (int64_t)(k - v.lo[2]) * v.len[1]);
-}
-
-// Reaction source wdot (chemistry.H compute_spec_source, table form of
-// py_utils/rxnscheme_writer/example/chemistry.H:27-54).  Rate constant:
-// A_r, or A_r exp(-Ea_r/(RU T)) when Ea_r != 0.  Integer reaction orders 1
-// and 2 are exact products (pow(c,1) = c, pow(c,2) = c*c).
-template <int NS>
-__device__ __forceinline__ void spec_source(const double* spec, double temp, double* wdot) {
-    const DevParams& P = c_P;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) wdot[s] = 0.0;
-    if (!P.chem_on) return;
-    for (int r = 0; r < P.nreact; ++r) {
-        double cm = 1.0;
-#pragma unroll
-        for (int s = 0; s < NS; ++s) {
-            const double o = P.order[r][s];
-            if (s < P.nspec && o > 0.0) {
-                const double c = spec[s];
-                cm *= (o == 1.0) ? c : (o == 2.0) ? c * c : pow(c, o);
-            }
-        }
-        double kr = P.A[r];
-        if (P.Ea[r] != 0.0) kr = P.A[r] * exp(-P.Ea[r] / (kRU * temp));
-        const double rate = kr * cm;
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-            if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) wdot[s] += P.nu[r][s] * rate;
-    }
-}
-
 template <int NS>
 __global__ void chem_source_kernel(Valid v, Fab S, Fab D) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= v.n) return;
-    int i, j, k;
-    cell_of(v, t, i, j, k);
-    double spec[NS], w[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) spec[s] = (s < c_P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
-    spec_source<NS>(spec, S(i, j, k, TEMP), w);
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-        if (s < c_P.nspec) D(i, j, k, NFLO + s) = add(D(i, j, k, NFLO + s), add(0.0, w[s]));
+    chem_source_body<NS>(v, S, D, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
-
-// SSP-RK3 sub-step of the reaction source for one cell, all three stages in
-// registers (the chemistry right-hand side is local to the cell).  Stage
-// states S_i = S_old + sum_j (dt*a_ij) F_j, result S_old + sum_i (dt*w_i) F_i
-// (AMReX RKIntegrator with the SSPRK3 tableau: a21=1, a31=a32=1/4,
-// w=1/6,1/6,2/3).  Components without a source keep S_old.
 template <int NS>
 __global__ void chem_substep_kernel(Valid v, Fab So, Fab Sn, double dt, int ncomp) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= v.n) return;
-    int i, j, k;
-    cell_of(v, t, i, j, k);
-    const int ns = c_P.nspec;
-    double s0[NS], s1[NS], f0[NS], f1[NS], f2[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) s0[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
-    const double temp = So(i, j, k, TEMP);
-    spec_source<NS>(s0, temp, f0);
-    const double c10 = dt * 1.0, c20 = dt * 0.25, c21 = dt * 0.25;
-#pragma unroll
-    for (int s = 0; s < NS; ++s) s1[s] = add(s0[s], mul(c10, add(0.0, add(0.0, f0[s]))));
-    spec_source<NS>(s1, temp, f1);
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-        s1[s] = add(add(s0[s], mul(c20, add(0.0, add(0.0, f0[s])))), mul(c21, add(0.0, add(0.0, f1[s]))));
-    spec_source<NS>(s1, temp, f2);
-    const double w0 = dt * (1.0 / 6.0), w1 = dt * (1.0 / 6.0), w2 = dt * (2.0 / 3.0);
-    for (int n = 0; n < ncomp; ++n) {
-        if (n >= NFLO) continue;
-        Sn(i, j, k, n) = So(i, j, k, n);
-    }
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-        if (s >= ns) continue;
-        double r = s0[s];
-        r = add(r, mul(w0, add(0.0, add(0.0, f0[s]))));
-        r = add(r, mul(w1, add(0.0, add(0.0, f1[s]))));
-        r = add(r, mul(w2, add(0.0, add(0.0, f2[s]))));
-        Sn(i, j, k, NFLO + s) = r;
-    }
+    chem_substep_body<NS>(v, So, Sn, dt, ncomp, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
-
-// cons -> prim refresh (Source/mflo_evolve.cpp:114-171); negative pressure
-// raises a status bit instead of aborting.
 template <int NS>
 __global__ void prims_kernel(Valid v, Fab S) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= v.n) return;
-    int i, j, k;
-    cell_of(v, t, i, j, k);
-    const DevParams& P = c_P;
-    const double vf = S(i, j, k, VFRAC);
-    if (vf == 1.0) {
-        const double rho = S(i, j, k, RHO);
-        double spec[NS];
-#pragma unroll
-        for (int s = 0; s < NS; ++s) spec[s] = (s < P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
-        const double vx = S(i, j, k, RHOU) / rho, vy = S(i, j, k, RHOV) / rho, vz = S(i, j, k, RHOW) / rho;
-        const double rhoe = S(i, j, k, RHOE) - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
-        const double p = thermo_p<NS>(rhoe, rho, spec);
-        S(i, j, k, DENS) = rho;
-        S(i, j, k, VELX) = vx;
-        S(i, j, k, VELY) = vy;
-        S(i, j, k, VELZ) = vz;
-        S(i, j, k, PRES) = p;
-        S(i, j, k, TEMP) = thermo_t<NS>(rho, p, spec);
-    } else if (P.conj_ht && vf == 0.0) {
-        S(i, j, k, TEMP) = P.solid_temp;
-    }
-    if (P.do_ns && S(i, j, k, PRES) < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
+    prims_body<NS>(v, S, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
-
 __global__ void clip_kernel(Valid v, Fab S, int nspec) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= v.n) return;
-    int i, j, k;
-    cell_of(v, t, i, j, k);
-    for (int s = 0; s < nspec; ++s)
-        if (S(i, j, k, NFLO + s) < 0.0) S(i, j, k, NFLO + s) = 0.0;
+    clip_body(v, S, nspec, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Block partial sums of ((s_new - s_old)/dt [* vfrac_old])^2 per component;

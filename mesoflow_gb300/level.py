@@ -158,3 +158,55 @@ def geometry(domain_lo, domain_hi, prob_lo, prob_hi, periodic):
         g.domain_hi[d] = domain_hi[d]
         g.is_periodic[d] = 1 if periodic[d] else 0
     return g
+
+
+class MultiLevel:
+    """Boxes of several levels in one descriptor array (mfg_box.level set), for
+    the batched entry points.  backend: 'numpy' or 'torch'."""
+
+    def __init__(self, amr, backend="torch", device=None):
+        self.amr = amr
+        self.ncomp = amr.ncomp
+        self.levels = []
+        self.index = []  # global box -> (level, local box)
+        for l in range(len(amr.geoms)):
+            bl = [(lo, hi) for lo, hi, lv in amr.boxes if lv == l]
+            self.levels.append(Level(bl, amr.ncomp, backend=backend, device=device, with_dsdt=False))
+        counters = [0] * len(amr.geoms)
+        for lo, hi, lv in amr.boxes:
+            self.index.append((lv, counters[lv]))
+            counters[lv] += 1
+        self.set_states(amr.states)
+        self._desc = None
+
+    def set_states(self, states):
+        for (lv, b), s in zip(self.index, states):
+            lev = self.levels[lv]
+            if lev.backend == "numpy":
+                lev.s_new[b][...] = s
+            else:
+                import torch
+                lev.s_new[b].copy_(torch.as_tensor(np.ascontiguousarray(s), device=lev.device))
+
+    def descriptors(self):
+        if self._desc is not None:
+            return self._desc
+        per = [lev.descriptors() for lev in self.levels]
+        arr = (abi.Box * len(self.index))()
+        for g, (lv, b) in enumerate(self.index):
+            arr[g] = per[lv][b]
+            arr[g].level = lv
+        self._desc = arr
+        return arr
+
+    def geoms(self):
+        arr = (abi.Geom * len(self.amr.geoms))()
+        for l, g in enumerate(self.amr.geoms):
+            arr[l] = g
+        return arr
+
+    def box_state(self, g, which="new"):
+        lv, b = self.index[g]
+        lev = self.levels[lv]
+        a = (lev.s_new if which == "new" else lev.s_old)[b]
+        return a if lev.backend == "numpy" else a.detach().cpu().numpy()
