@@ -16,6 +16,7 @@ host cores.
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -226,6 +227,83 @@ def run_amr(a):
     return 0
 
 
+def run_adjoint(a):
+    """Adjoint form: wall time of one gradient evaluation (J, dJ/dlog A_r for 8
+    reactions and dJ/du_in through the hand-written adjoint of the whole step)
+    against the same nsteps plain steps plus the objective, on the catalyst
+    case (8 gas + 2 site species, WENO5, velocity inlet) at n^3 in 32^3 boxes.
+    Both with every step's intermediates kept in HBM (checkpoint_every 0) and
+    with checkpoints every 5 steps (recomputation)."""
+    import torch
+    from mesoflow_gb300 import abi, cases
+    from mesoflow_gb300.adjoint import ReactionProblem
+    from mesoflow_gb300.driver import Mflo
+    torch.cuda.set_device(0)
+    lib = abi.load()
+    n = a.n if a.n != 256 else 128
+    case = cases.catalyst(n=n, order=5, max_grid=32)
+    nsteps = a.adj_steps
+    dt = Mflo(case, device="cuda:0").est_timestep()
+    logA = [math.log(case.params.A[r]) for r in range(case.params.nreact)]
+    u_in = case.meta["u_in"]
+    nb = len(case.boxes)
+    g = C.byref(case.geom)
+
+    def timed(p, fn):
+        p.reset(logA, u_in)
+        torch.cuda.synchronize()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        fn(p, C.c_void_p(s.cuda_stream))
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def forward(p, st):
+        for i in range(nsteps):
+            abi.check("mfg_advance_level", lib.mfg_advance_level(p.desc, nb, g, i * dt, dt, 0, 1, None, st))
+        J = C.c_double()
+        abi.check("mfg_reaction_objective", lib.mfg_reaction_objective(p.desc, nb, g, C.byref(J), st))
+
+    def adjoint(ce):
+        def fn(p, st):
+            J, gu = C.c_double(), C.c_double()
+            gA = (C.c_double * 16)()
+            abi.check("mfg_adjoint_objective", lib.mfg_adjoint_objective(p.desc, nb, g, nsteps, dt, ce, C.byref(J),
+                                                                         gA, C.byref(gu), st))
+        return fn
+
+    p = ReactionProblem(case, nsteps, dt)
+    reps = max(1, a.steps // 2)
+    res = {}
+    for name, fn in (("forward", forward), ("adjoint_keep_all", adjoint(0)), ("adjoint_checkpoint5", adjoint(5))):
+        for _ in range(1):
+            timed(p, fn)
+        ms = sorted(timed(p, fn) for _ in range(reps))
+        res[name] = ms[len(ms) // 2]
+    lib.mfg_profile(1)
+    timed(p, adjoint(0))
+    kk = 32
+    kms, kcnt = (C.c_double * kk)(), (C.c_longlong * kk)()
+    nk = lib.mfg_profile_read(kms, kcnt, kk)
+    lib.mfg_profile(0)
+    kernels = {lib.mfg_profile_name(i).decode(): {"ms": kms[i], "launches": kcnt[i]} for i in range(nk) if kcnt[i]}
+    cells = n ** 3
+    out = {"metric": "adjoint / forward wall-time ratio (gradient of the surface reaction rate)",
+           "value": res["adjoint_keep_all"] / res["forward"], "unit": "x", "higher_is_better": False,
+           "n_gpus": 1, "steps": reps, "warmup": 1, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"catalyst {n}^3 in {nb} boxes of 32^3, 8 gas + 2 site species, 8 Arrhenius "
+                                  f"surface reactions, WENO5, velocity inlet, {nsteps} steps of dt {dt:.3e}",
+                      "gradient": "J and dJ/dlog A_r (8) and dJ/du_in"},
+           "ms": res,
+           "ratio_checkpoint5": res["adjoint_checkpoint5"] / res["forward"],
+           "gradient_cell_steps_per_s": cells * nsteps / (res["adjoint_keep_all"] / 1e3),
+           "kernels_keep_all": kernels}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,15 +314,19 @@ def main():
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--max-grid", dest="max_grid", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--workload", default="ib", choices=["ib", "tg", "amr"],
+    ap.add_argument("--workload", default="ib", choices=["ib", "tg", "amr", "adjoint"],
                     help="ib: the 256^3 immersed-boundary workload (default); tg: 256^3 5-species Taylor-Green "
-                         "(use --order 5); amr: batched vs plain on 3 levels")
+                         "(use --order 5); amr: batched vs plain on 3 levels; adjoint: gradient vs forward time "
+                         "on the catalyst case (--n, default 128)")
+    ap.add_argument("--adj-steps", dest="adj_steps", type=int, default=10)
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     if a.impl == "reference":
         return run_reference(a)
     if a.workload == "amr":
         return run_amr(a)
+    if a.workload == "adjoint":
+        return run_adjoint(a)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -332,7 +414,7 @@ def main():
     # ---- per-kernel timing (CUDA events on the launching stream) -----------------
     lib.mfg_profile(1)
     step(t)
-    kk = 16
+    kk = 32
     kms = (C.c_double * kk)()
     kcnt = (C.c_longlong * kk)()
     nk = lib.mfg_profile_read(kms, kcnt, kk)

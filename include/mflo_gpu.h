@@ -332,6 +332,37 @@ int mfg_boxlist_autotune(mfg_boxlist* list, double dt, double* results, void* st
 /* Number of valid cells in the list. */
 long long mfg_boxlist_cells(const mfg_boxlist* list);
 
+/* ---- adjoint form --------------------------------------------------------------
+ * No counterpart in the reference (its solver is forward only).  The
+ * objective is the integrated surface reaction rate
+ *     J = dx dy dz * sum_valid_cells sum_r k_r(T) prod_s c_s^order[r][s]
+ * with k_r = A_r, or A_r exp(-Ea_r/(RU T)) when Ea_r != 0 (the rate law of
+ * the chemistry source, chemistry.H compute_spec_source). */
+
+/* J on the boxes' s_new.  Synchronizes. */
+int mfg_reaction_objective(const mfg_box* boxes, int nbox, const mfg_geom* geom, double* J,
+                           void* stream);
+
+/* Advances the level nsteps steps of dt from s_new, exactly as nsteps calls of
+ * mfg_advance_level(only_flow = 0, clip = 1), evaluates J on the result and
+ * returns it with its gradients from a hand-written discrete adjoint of the
+ * whole step: grad_logA[r] = dJ/dlog A_r (nreact values), grad_uin = dJ/d(the
+ * normal velocity of the velocity-inlet boundaries, the initial state held
+ * fixed).  Both gradient pointers may be null.  checkpoint_every > 0: the
+ * state is kept every checkpoint_every steps and the steps between are
+ * recomputed during the reverse sweep (device memory: about
+ * nsteps/checkpoint_every + checkpoint_every + 10 level-sized arrays and 5
+ * grown ones); checkpoint_every = 0: every step's intermediates are kept and
+ * nothing is recomputed (about 3 level-sized and 3 grown arrays per step).
+ * The gradients do not depend on the choice beyond rounding.  Supported: order_hyp 5,
+ * do_ns 1, molar or mass-single thermo, constant viscosity and conductivity,
+ * no conj_ht, ext_dir boundaries of kind VELOCITY_INLET or FIXED_STATE; other
+ * configurations return MFG_ERR_STATE.  On return s_new holds the state after
+ * nsteps; s_old and sborder hold intermediates.  Synchronizes. */
+int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_geom* geom, int nsteps,
+                          double dt, int checkpoint_every, double* J, double* grad_logA,
+                          double* grad_uin, void* stream);
+
 /* ---- diagnostics (no counterpart in the reference beyond BL_PROFILE) ------ */
 
 /* Enables (1) or disables (0) CUDA-event timing of every kernel launch and
@@ -344,6 +375,9 @@ int mfg_profile_read(double* ms, long long* count, int nkinds);
 
 /* Name of a kernel kind of mfg_profile_read. */
 const char* mfg_profile_name(int kind);
+
+/* Description of the last failed CUDA call behind an MFG_ERR_CUDA ("" if none). */
+const char* mfg_last_error(void);
 
 /* Total kernel launches issued by the library since it was loaded. */
 unsigned long long mfg_launch_count(void);

@@ -28,7 +28,7 @@ EXT_FIXED_STATE, EXT_PRESSURE_INLET, EXT_PRESSURE_OUTLET, EXT_VELOCITY_INLET = 0
 ERROR_NAMES = {
     OK: "ok", ERR_ARG: "bad argument", ERR_NAN: "NaN detected in dsdt",
     ERR_NEG_PRESSURE: "Pressure has gone negative", ERR_SCHEME: "unknown hyperbolics scheme",
-    ERR_TIMEOUT: "device wait timed out", ERR_CUDA: "CUDA error", ERR_STATE: "library not initialised",
+    ERR_TIMEOUT: "device wait timed out", ERR_CUDA: "CUDA error", ERR_STATE: "library not initialised or configuration not supported",
     ERR_SIZE: "box needs more scratch than the static array of the allocation-free entry point",
 }
 
@@ -110,6 +110,11 @@ SIGNATURES = [
     ("mfg_boxlist_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
     ("mfg_boxlist_autotune", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), _VP]),
     ("mfg_boxlist_cells", C.c_longlong, [C.c_void_p]),
+    ("mfg_last_error", C.c_char_p, []),
+    ("mfg_reaction_objective", C.c_int, [_BP, C.c_int, _GP, C.POINTER(C.c_double), _VP]),
+    ("mfg_adjoint_objective", C.c_int, [_BP, C.c_int, _GP, C.c_int, C.c_double, C.c_int,
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), _VP]),
 ]
 
 _lib = None
@@ -136,7 +141,12 @@ def load(path=None):
 
 class MfloError(RuntimeError):
     def __init__(self, call, code):
-        super().__init__(f"{call} failed: {ERROR_NAMES.get(code, code)} (status {code})")
+        msg = f"{call} failed: {ERROR_NAMES.get(code, code)} (status {code})"
+        if code == ERR_CUDA and _lib is not None:
+            detail = _lib.mfg_last_error()
+            if detail:
+                msg += f" [{detail.decode()}]"
+        super().__init__(msg)
         self.code = code
 
 

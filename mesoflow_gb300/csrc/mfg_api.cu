@@ -78,7 +78,13 @@ int check_boxes(const mfg_box* boxes, int nbox, bool need_sb, bool need_dsdt, bo
     return MFG_OK;
 }
 
-int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MFG_OK : MFG_ERR_CUDA; }
+char g_last_error[256] = "";
+
+int cuda_rc(cudaError_t e) {
+    if (e == cudaSuccess) return MFG_OK;
+    note_cuda_error(e, "fill patch");
+    return MFG_ERR_CUDA;
+}
 
 size_t rhs_scratch_doubles(const int n[3]) {
     size_t s = aux_doubles(n);
@@ -139,6 +145,10 @@ int run_rhs(const mfg_box* boxes, int nbox, const mfg_geom* geom, int stage, dou
 
 const DevParams& c_host_params() { return g_hp; }
 
+void note_cuda_error(cudaError_t e, const char* where) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
+}
+
 // Shared with the allocation-free entry point (mfg_noalloc.cu).
 int validate_boxes(const mfg_box* boxes, int nbox, bool need_sb, bool need_dsdt, bool need_old, bool need_new) {
     return check_boxes(boxes, nbox, need_sb, need_dsdt, need_old, need_new);
@@ -154,6 +164,8 @@ using namespace mfg;
 extern "C" {
 
 const char* mfg_version(void) { return "mesoflow-gb300 0.1 (sm_103a, FP64)"; }
+
+const char* mfg_last_error(void) { return g_last_error; }
 
 int mfg_init(const mfg_params* p) {
     if (!p) return MFG_ERR_ARG;

@@ -27,7 +27,9 @@ enum FsComp {
 // Kernel kinds of the launch counter / event profiler (mfg_prof.cu).
 enum KernelKind {
     K_PRIM = 0, K_FACE, K_FLUX, K_UPDATE, K_FILL_COPY, K_FILL_BC, K_CUT, K_CHEM, K_PRIMS, K_CLIP,
-    K_RESNORM, K_TIMESTEP, K_COPY, K_COUNT
+    K_RESNORM, K_TIMESTEP, K_COPY,
+    // adjoint (mfg_adjoint.cu)
+    K_ADJ_FACE, K_ADJ_CELL, K_ADJ_CUT, K_ADJ_FILL, K_ADJ_LOCAL, K_SNAPSHOT, K_ADJ_FLUX, K_ADJ_FACE_FWD, K_COUNT
 };
 
 // Counts one launch; when profiling is on, brackets it with CUDA events on its stream.
@@ -65,6 +67,9 @@ bool weno_fast_mode();
 
 cudaError_t upload_params(const DevParams& h);
 cudaError_t read_status(unsigned* v, bool clear);
+
+// Records the description of a failed CUDA call for mfg_last_error (mfg_api.cu).
+void note_cuda_error(cudaError_t e, const char* where);
 cudaError_t launch_rhs_box(const RhsBox& B, int stage, double dt, bool fast, cudaStream_t st);
 
 // Scratch sizes (doubles) for a box of the given valid extent.

@@ -8,7 +8,9 @@ namespace mfg {
 namespace {
 
 const char* kNames[K_COUNT] = {"prim", "face", "flux", "update", "fill_copy", "fill_bc",
-                               "cutcell", "chem", "prims", "clip", "resnorm", "timestep", "copy"};
+                               "cutcell", "chem", "prims", "clip", "resnorm", "timestep", "copy",
+                               "adj_face", "adj_cell", "adj_cut", "adj_fill", "adj_local", "snapshot",
+                               "adj_flux", "adj_face_fwd"};
 
 struct Pending {
     int kind;

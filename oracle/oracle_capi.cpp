@@ -598,3 +598,31 @@ extern "C" int oracle_abi_layout(int64_t* out, int n) {
     for (int i = 0; i < m && i < n; i++) out[i] = v[i];
     return m;
 }
+
+// Integrated surface reaction rate J = V_cell * sum_cells sum_r rate_r (the
+// differentiation objective): rate_r = k_r(T) prod_j c_j^order_rj on s_new,
+// k_r = A_r exp(-Ea_r/(RU T)), T the temperature component.
+extern "C" int oracle_objective(const mfg_params* P, const mfg_geom* G, const mfg_box* boxes, int nbox, double* J) {
+    double acc = 0.0;
+    const double vol = G->dx[0] * G->dx[1] * G->dx[2];
+    for (int ib = 0; ib < nbox; ib++) {
+        const mfg_box& b = boxes[ib];
+        A4 s(b.s_new);
+        for (int k = b.lo[2]; k <= b.hi[2]; k++)
+            for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                for (int i = b.lo[0]; i <= b.hi[0]; i++) {
+                    double cell = 0.0;
+                    for (int r = 0; r < P->nreact; r++) {
+                        double cm = 1.0;
+                        for (int sp = 0; sp < P->nspec; sp++)
+                            if (P->order[r][sp] > 0.0) cm *= std::pow(s(i, j, k, FLO_NVARS + sp), P->order[r][sp]);
+                        double kr = P->A[r];
+                        if (P->Ea[r] != 0.0) kr = P->A[r] * std::exp(-P->Ea[r] / (RU * s(i, j, k, TEMP_INDX)));
+                        cell += kr * cm;
+                    }
+                    acc += cell;
+                }
+    }
+    *J = acc * vol;
+    return MFG_OK;
+}

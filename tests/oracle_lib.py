@@ -34,6 +34,7 @@ def load(variant="strict"):
         "oracle_est_timestep": [PP, GP, BP, C.c_int, C.POINTER(C.c_double)],
         "oracle_advance": [PP, GP, BP, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)],
         "oracle_abi_layout": [C.POINTER(C.c_int64), C.c_int],
+        "oracle_objective": [PP, GP, BP, C.c_int, C.POINTER(C.c_double)],
     }
     for k, v in sig.items():
         f = getattr(lib, k)
