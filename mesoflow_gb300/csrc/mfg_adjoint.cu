@@ -885,12 +885,25 @@ __device__ __forceinline__ double dcpow(double c, double o) {
     return (o == 1.0) ? 1.0 : (o == 2.0) ? 2.0 * c : o * pow(c, o - 1.0);
 }
 
-// Rate of reaction r at (c, T) (spec_source's k_r prod c^o) with d rate/dc_j and d rate/dT.
+// Rate constants at T (spec_source's k_r = A_r, or A_r exp(-Ea_r/(RU T))) and
+// d log k_r / dT = Ea_r/(RU T^2); T is fixed through a chemistry sub-step.
 template <int NS>
-__device__ double rate_r(int r, const double* c, double T, double* dc, double& dT) {
+__device__ void rate_constants(double T, double* kr, double* eT) {
     const DevParams& P = c_P;
-    double kr = P.A[r];
-    if (P.Ea[r] != 0.0) kr = P.A[r] * exp(-P.Ea[r] / (kRU * T));
+    for (int r = 0; r < P.nreact; ++r) {
+        kr[r] = P.A[r];
+        eT[r] = 0.0;
+        if (P.Ea[r] != 0.0) {
+            kr[r] = P.A[r] * exp(-P.Ea[r] / (kRU * T));
+            eT[r] = P.Ea[r] / (kRU * T * T);
+        }
+    }
+}
+
+// Rate of reaction r (k_r prod c^o) with d rate/dc_j.
+template <int NS>
+__device__ double rate_k(int r, double kr, const double* c, double* dc) {
+    const DevParams& P = c_P;
     double cm = 1.0;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -910,15 +923,34 @@ __device__ double rate_r(int r, const double* c, double T, double* dc, double& d
         }
         dc[j] = pr;
     }
-    const double rate = kr * cm;
-    dT = (P.Ea[r] != 0.0) ? rate * P.Ea[r] / (kRU * T * T) : 0.0;
-    return rate;
+    return kr * cm;
+}
+
+// wdot with given rate constants (spec_source without the exponentials).
+template <int NS>
+__device__ void wdot_k(const double* c, const double* kr, double* w) {
+    const DevParams& P = c_P;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) w[s] = 0.0;
+    for (int r = 0; r < P.nreact; ++r) {
+        double cm = 1.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const double o = P.order[r][s];
+            if (s < P.nspec && o > 0.0) cm *= cpow(c[s], o);
+        }
+        const double rate = kr[r] * cm;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) w[s] += P.nu[r][s] * rate;
+    }
 }
 
 // wdot = sum_r nu_r rate_r reversed for the adjoint fb of wdot: species into
 // cb, temperature into Tb, d/dlog A_r (= rate_r times the seed) into thb.
 template <int NS>
-__device__ void wdot_vjp(const double* c, double T, const double* fb, double* cb, double& Tb, double* thb) {
+__device__ void wdot_vjp(const double* c, const double* kr, const double* eT, const double* fb, double* cb,
+                         double& Tb, double* thb) {
     const DevParams& P = c_P;
     for (int r = 0; r < P.nreact; ++r) {
         double rb = 0.0;
@@ -926,10 +958,10 @@ __device__ void wdot_vjp(const double* c, double T, const double* fb, double* cb
         for (int s = 0; s < NS; ++s)
             if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) rb += P.nu[r][s] * fb[s];
         if (rb == 0.0) continue;
-        double dc[NS], dT;
-        const double rate = rate_r<NS>(r, c, T, dc, dT);
+        double dc[NS];
+        const double rate = rate_k<NS>(r, kr[r], c, dc);
         thb[r] += rb * rate;
-        Tb += rb * dT;
+        Tb += (rb * rate) * eT[r];
 #pragma unroll
         for (int j = 0; j < NS; ++j) cb[j] += rb * dc[j];
     }
@@ -960,12 +992,14 @@ __global__ void adj_chem_kernel(Valid v, Fab S3, Fab lam, double dt, double* gth
             snb[s] = (s < ns) ? lam(i, j, k, NFLO + s) : 0.0;
         }
         const double T = S3(i, j, k, TEMP);
+        double kr[MAXR], eT[MAXR];
+        rate_constants<NS>(T, kr, eT);
         const double c10 = dt * 1.0, c20 = dt * 0.25, c21 = dt * 0.25;
         const double w0 = dt * (1.0 / 6.0), w1 = dt * (1.0 / 6.0), w2 = dt * (2.0 / 3.0);
-        spec_source<NS>(s0, T, f0);
+        wdot_k<NS>(s0, kr, f0);
 #pragma unroll
         for (int s = 0; s < NS; ++s) s1[s] = s0[s] + c10 * f0[s];
-        spec_source<NS>(s1, T, f1);
+        wdot_k<NS>(s1, kr, f1);
 #pragma unroll
         for (int s = 0; s < NS; ++s) s2[s] = (s0[s] + c20 * f0[s]) + c21 * f1[s];
         double Tb = 0.0;
@@ -979,20 +1013,20 @@ __global__ void adj_chem_kernel(Valid v, Fab S3, Fab lam, double dt, double* gth
             s1b[s] = 0.0;
             s2b[s] = 0.0;
         }
-        wdot_vjp<NS>(s2, T, f2b, s2b, Tb, thb);
+        wdot_vjp<NS>(s2, kr, eT, f2b, s2b, Tb, thb);
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             s0b[s] += s2b[s];
             f0b[s] += c20 * s2b[s];
             f1b[s] += c21 * s2b[s];
         }
-        wdot_vjp<NS>(s1, T, f1b, s1b, Tb, thb);
+        wdot_vjp<NS>(s1, kr, eT, f1b, s1b, Tb, thb);
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             s0b[s] += s1b[s];
             f0b[s] += c10 * s1b[s];
         }
-        wdot_vjp<NS>(s0, T, f0b, s0b, Tb, thb);
+        wdot_vjp<NS>(s0, kr, eT, f0b, s0b, Tb, thb);
         for (int s = 0; s < ns; ++s) lam(i, j, k, NFLO + s) = s0b[s];
         lam(i, j, k, TEMP) += Tb;
     }
@@ -1011,18 +1045,20 @@ __global__ void objective_kernel(Valid v, Fab S, Fab lam, double vol, double* Ja
         int i, j, k;
         cell_of(v, t, i, j, k);
         const int ns = P.nspec;
-        double c[NS], cb[NS], dc[NS], dT, Tb = 0.0;
+        double c[NS], cb[NS], dc[NS], Tb = 0.0;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             c[s] = (s < ns) ? S(i, j, k, NFLO + s) : 0.0;
             cb[s] = 0.0;
         }
         const double T = S(i, j, k, TEMP);
+        double kr[MAXR], eT[MAXR];
+        rate_constants<NS>(T, kr, eT);
         for (int r = 0; r < P.nreact; ++r) {
-            const double rate = rate_r<NS>(r, c, T, dc, dT);
+            const double rate = rate_k<NS>(r, kr[r], c, dc);
             jloc += rate;
             th[r] = vol * rate;
-            Tb += vol * dT;
+            Tb += vol * (rate * eT[r]);
 #pragma unroll
             for (int s = 0; s < NS; ++s) cb[s] += vol * dc[s];
         }
