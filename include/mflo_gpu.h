@@ -287,6 +287,17 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom,
  * four reciprocals (flux_schemes.H:407-414) operation for operation. */
 int mfg_set_weno_mode(int fast);
 
+/* The cut-cell lists and inverse-distance weights depend on the volume
+ * fraction only, which the solver never changes; update_cutcells
+ * (ib_utils.H:272-436) recomputes them every stage.  With the cache on
+ * (default) the first mfg_cutcells / mfg_advance_level call for a box keeps
+ * them in device memory (synchronizes once; about 1 KiB per cut cell), and
+ * every later call checks the box's grown volume fraction against a stored
+ * copy on the device (exact) before using them: a changed geometry falls back
+ * to recomputation in the same call and is dropped from the cache.  Results
+ * are bitwise the same either way.  enable = 0 frees the cache.  Synchronizes. */
+int mfg_set_cutcell_cache(int enable);
+
 /* Same result as mfg_compute_dsdt_flow, for callers that may not allocate
  * device memory (for example an AMReX application, whose arena reserves most
  * of the GPU at start-up, or a code with a fixed device-memory budget): the

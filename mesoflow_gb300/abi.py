@@ -99,6 +99,7 @@ SIGNATURES = [
     ("mfg_advance_level", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.POINTER(C.c_double), _VP]),
     ("mfg_set_weno_mode", C.c_int, [C.c_int]),
+    ("mfg_set_cutcell_cache", C.c_int, [C.c_int]),
     ("mfg_profile", C.c_int, [C.c_int]),
     ("mfg_profile_read", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
     ("mfg_profile_name", C.c_char_p, [C.c_int]),

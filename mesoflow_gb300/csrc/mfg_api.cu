@@ -253,6 +253,7 @@ int mfg_finalize(void) {
     if (g_pool.p) cudaFree(g_pool.p);
     g_pool = Pool();
     fill_release();
+    cutcache_release();
     g_ready = false;
     return MFG_OK;
 }
@@ -443,7 +444,14 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, doub
     if (resnorms && (rc = mfg_residual_norms(boxes, nbox, dt, resnorms, stream))) return rc;
     unsigned v = 0;
     if (cudaStreamSynchronize(st) != cudaSuccess || read_status(&v, false) != cudaSuccess) return MFG_ERR_CUDA;
+    cutcache_sweep();
     if (v & MFG_STATUS_NAN) return MFG_ERR_NAN;
+    return MFG_OK;
+}
+
+int mfg_set_cutcell_cache(int enable) {
+    if (cudaDeviceSynchronize() != cudaSuccess) return MFG_ERR_CUDA;
+    cutcache_enable(enable != 0);
     return MFG_OK;
 }
 

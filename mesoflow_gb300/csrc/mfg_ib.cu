@@ -12,11 +12,22 @@
 //
 // Work layout: a compaction pass lists the box's cut cells (one atomic per
 // warp), then a fixed grid of threads walks the list, one cut cell per thread,
-// so no lane idles on pure fluid or solid cells.  Each neighbour's weight
-// 1/(d^2 + 1e-40) is computed once (Newton-refined reciprocal) and shared by
-// all interpolated components (the reference divides per component); the
-// Dirichlet weights depend only on the grid and come from a constant table.
+// so no lane idles on pure fluid or solid cells.
+//
+// Cut-cell cache: the list and the weights depend on the volume fraction of
+// the grown box only, which the solver never changes, while the reference
+// recomputes them for every stage of every step.  The first call for a box
+// (keyed by its Sborder view and extent) keeps a copy of the grown volume
+// fraction, the list, and every cut cell's fluid-neighbour mask and weights.
+// Every later call first compares the volume fraction with the copy on the
+// device (exact, bit patterns); the cut-cell kernel uses the stored weights
+// when nothing changed and recomputes everything on the fly otherwise, so a
+// changed geometry is never served stale weights.  Both paths give bitwise
+// equal results.  Changed boxes are dropped from the cache by
+// cutcache_sweep (called where the host synchronizes anyway).
 #include <algorithm>
+#include <unordered_map>
+#include <vector>
 
 #include "mfg_ib_body.cuh"
 
@@ -45,8 +56,11 @@ __global__ void cht_avg_kernel(CutBox c) {
     c.tcht[t] = sum / 26.0;
 }
 
-// Appends the linear index of every cut cell (0 < vfrac < 1) of the box to list.
-__global__ void cut_list_kernel(CutBox c, int* __restrict__ list, unsigned* __restrict__ count) {
+// Appends the linear index of every cut cell (0 < vfrac < 1) of the box to
+// list; with a non-null flag, only when *flag is set.
+__global__ void cut_list_kernel(CutBox c, int* __restrict__ list, unsigned* __restrict__ count,
+                                const unsigned* __restrict__ flag) {
+    if (flag && !*flag) return;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool cut = false;
     if (t < c.n) {
@@ -72,9 +86,195 @@ __global__ void __launch_bounds__(TPB) cutcell_kernel(CutBox c, const int* __res
         cutcell_one<NS>(c, list[w]);
 }
 
+// Grown-box volume fraction: copy (mode 0) or compare with the copy (mode 1,
+// sets *dirty on any difference of bit patterns).
+__global__ void cut_vf_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int l1, int l2, double* __restrict__ vf,
+                              unsigned* __restrict__ dirty, int mode) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool diff = false;
+    if (t < (int64_t)l0 * l1 * l2) {
+        const int64_t a = t / l0;
+        const int i = lo0 + (int)(t - a * l0), j = lo1 + (int)(a % l1), k = lo2 + (int)(a / l1);
+        const double v = S(i, j, k, VFRAC);
+        if (mode == 0)
+            vf[t] = v;
+        else
+            diff = __double_as_longlong(v) != __double_as_longlong(vf[t]);
+    }
+    if (mode == 1 && __any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(dirty, 1u);
+}
+
+__global__ void cut_weights_kernel(CutBox c, const int* __restrict__ list, unsigned n, unsigned long long* mask,
+                                   double* scal, double* wn) {
+    const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= n) return;
+    cut_weights_one(c, list[w], (int)w, mask, scal, wn);
+}
+
+// Stored weights when the volume fraction is unchanged (*dirty == 0), else the
+// on-the-fly form over the freshly built list.
+template <int NS>
+__global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, const int* __restrict__ clist, unsigned ncut,
+                                                             CutCacheView cc, const unsigned* __restrict__ dirty,
+                                                             const int* __restrict__ list,
+                                                             const unsigned* __restrict__ count) {
+    if (*dirty) {
+        const unsigned n = *count;
+        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+            cutcell_one<NS>(c, list[w]);
+        return;
+    }
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ncut; w += gridDim.x * blockDim.x)
+        cutcell_cached<NS>(c, clist[w], (int)w, cc);
+}
+
 double g_wdir_dx[3] = {-1.0, -1.0, -1.0};
 
+struct CutEntry {
+    int lo[3], hi[3];
+    int64_t js, ks, ns;
+    double dx[3];
+    double* vf = nullptr;
+    int* list = nullptr;
+    unsigned ncut = 0;
+    unsigned long long* mask = nullptr;
+    double* scal = nullptr;
+    double* wn = nullptr;
+    int slot = -1;  // index of this entry's flag in g_cache.dirty
+};
+
+struct CutCache {
+    std::unordered_map<const double*, CutEntry> map;
+    unsigned* dirty = nullptr;  // one flag per slot
+    unsigned* count = nullptr;  // build scratch
+    int nslots = 0, cap = 0;
+    std::vector<int> free_slots;
+    size_t bytes = 0;
+    bool enabled = true;
+} g_cache;
+
+void free_entry(CutEntry& e) {
+    cudaFree(e.vf);
+    cudaFree(e.list);
+    cudaFree(e.mask);
+    cudaFree(e.scal);
+    cudaFree(e.wn);
+    if (e.slot >= 0) g_cache.free_slots.push_back(e.slot);
+    e = CutEntry();
+}
+
+bool same_key(const CutEntry& e, const mfg_box& b, const Fab& S, const mfg_geom& g) {
+    for (int d = 0; d < 3; ++d)
+        if (e.lo[d] != b.lo[d] || e.hi[d] != b.hi[d] || e.dx[d] != g.dx[d]) return false;
+    return e.js == S.js && e.ks == S.ks && e.ns == S.ns;
+}
+
+int new_slot(cudaStream_t st) {
+    if (!g_cache.free_slots.empty()) {
+        const int s = g_cache.free_slots.back();
+        g_cache.free_slots.pop_back();
+        return s;
+    }
+    if (g_cache.nslots == g_cache.cap) {
+        const int cap = std::max(256, 2 * g_cache.cap);
+        unsigned* d = nullptr;
+        if (cudaMalloc(&d, cap * sizeof(unsigned)) != cudaSuccess) return -1;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+        if (g_cache.dirty) {
+            cudaMemcpy(d, g_cache.dirty, g_cache.cap * sizeof(unsigned), cudaMemcpyDeviceToDevice);
+            cudaFree(g_cache.dirty);
+        }
+        g_cache.dirty = d;
+        g_cache.cap = cap;
+    }
+    return g_cache.nslots++;
+}
+
+// Builds the cache entry of a box from its current Sborder (synchronizes once).
+bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry& e, cudaStream_t st) {
+    const int l0 = c.len[0] + 6, l1 = c.len[1] + 6, l2 = c.len[2] + 6;
+    const size_t ng = (size_t)l0 * l1 * l2;
+    for (int d = 0; d < 3; ++d) {
+        e.lo[d] = b.lo[d];
+        e.hi[d] = b.hi[d];
+        e.dx[d] = g.dx[d];
+    }
+    e.js = c.S.js;
+    e.ks = c.S.ks;
+    e.ns = c.S.ns;
+    if (!g_cache.count && cudaMalloc(&g_cache.count, sizeof(unsigned)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.vf, ng * sizeof(double)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.list, std::max<int64_t>(c.n, 1) * sizeof(int)) != cudaSuccess) return false;
+    cut_vf_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0, l1,
+                                                                 l2, e.vf, nullptr, 0);
+    cudaMemsetAsync(g_cache.count, 0, sizeof(unsigned), st);
+    cut_list_kernel<<<(unsigned)((c.n + TPB - 1) / TPB), TPB, 0, st>>>(c, e.list, g_cache.count, nullptr);
+    if (cudaMemcpyAsync(&e.ncut, g_cache.count, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return false;
+    const size_t n = std::max<unsigned>(e.ncut, 1);
+    const size_t need = n * (2 * sizeof(unsigned long long) + 2 * sizeof(double) + CUT_SLOTS * sizeof(double));
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || need > fr / 4) return false;  // leave room for the caller
+    if (cudaMalloc(&e.mask, n * 2 * sizeof(unsigned long long)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.scal, n * 2 * sizeof(double)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.wn, n * CUT_SLOTS * sizeof(double)) != cudaSuccess) return false;
+    if ((e.slot = new_slot(st)) < 0) return false;
+    if (e.ncut)
+        cut_weights_kernel<<<(e.ncut + TPB - 1) / TPB, TPB, 0, st>>>(c, e.list, e.ncut, e.mask, e.scal, e.wn);
+    g_cache.bytes += ng * sizeof(double) + c.n * sizeof(int) + need;
+    return cudaGetLastError() == cudaSuccess;
+}
+
+CutEntry* find_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, cudaStream_t st) {
+    if (!g_cache.enabled) return nullptr;
+    auto it = g_cache.map.find(c.S.p);
+    if (it != g_cache.map.end()) {
+        if (same_key(it->second, b, c.S, g)) return &it->second;
+        free_entry(it->second);
+        g_cache.map.erase(it);
+    }
+    CutEntry e;
+    if (!build_entry(b, c, g, e, st)) {
+        cudaGetLastError();  // an allocation refused here is not an error of the step
+        free_entry(e);
+        return nullptr;
+    }
+    return &(g_cache.map[c.S.p] = e);
+}
+
 }  // namespace
+
+// Drops the entries whose volume fraction changed in the last call; the host
+// has synchronized the stream before.
+void cutcache_sweep() {
+    if (g_cache.map.empty() || !g_cache.dirty) return;
+    std::vector<unsigned> h(g_cache.nslots);
+    if (cudaMemcpy(h.data(), g_cache.dirty, h.size() * sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return;
+    for (auto it = g_cache.map.begin(); it != g_cache.map.end();) {
+        if (it->second.slot >= 0 && h[it->second.slot]) {
+            free_entry(it->second);
+            it = g_cache.map.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+void cutcache_release() {
+    for (auto& kv : g_cache.map) free_entry(kv.second);
+    g_cache.map.clear();
+    cudaFree(g_cache.dirty);
+    cudaFree(g_cache.count);
+    const bool en = g_cache.enabled;
+    g_cache = CutCache();
+    g_cache.enabled = en;
+}
+
+void cutcache_enable(bool on) {
+    if (!on) cutcache_release();
+    g_cache.enabled = on;
+}
 
 cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, int* list,
                                 unsigned* count, cudaStream_t st) {
@@ -106,15 +306,34 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
         if (e != cudaSuccess) return e;
         cudaStreamSynchronize(st);
         for (int d = 0; d < 3; ++d) g_wdir_dx[d] = dnk[d];
+        cutcache_release();  // stored weights used the previous table
     }
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
+    const int ns = c_host_params().nspec;
+    CutEntry* ce = find_entry(b, c, g, st);
     ProfScope ps(K_CUT, st);
     if (c_host_params().conj_ht) cht_avg_kernel<<<nb, TPB, 0, st>>>(c);
     cudaMemsetAsync(count, 0, sizeof(unsigned), st);
-    cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count);
+    if (ce) {
+        unsigned* dirty = g_cache.dirty + ce->slot;
+        const int l0 = c.len[0] + 6, l1 = c.len[1] + 6, l2 = c.len[2] + 6;
+        const int64_t ngc = (int64_t)l0 * l1 * l2;
+        cudaMemsetAsync(dirty, 0, sizeof(unsigned), st);
+        cut_vf_kernel<<<(unsigned)((ngc + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0,
+                                                                      l1, l2, ce->vf, dirty, 1);
+        cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, dirty);
+        const CutCacheView cv = {ce->mask, ce->scal, ce->wn};
+        const unsigned ng = (unsigned)std::min<int64_t>(std::max<int64_t>(nb, 1), 152 * 8);
+        if (ns <= 1) cutcell_cached_kernel<1><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        else if (ns <= 2) cutcell_cached_kernel<2><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        else if (ns <= 4) cutcell_cached_kernel<4><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        else if (ns <= 8) cutcell_cached_kernel<8><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        else cutcell_cached_kernel<16><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        return cudaGetLastError();
+    }
+    cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, nullptr);
     // a fixed grid walks the list (its length stays on the device)
     const unsigned ng = (unsigned)std::min<int64_t>(nb, 152 * 8);
-    const int ns = c_host_params().nspec;
     if (ns <= 1) cutcell_kernel<1><<<ng, TPB, 0, st>>>(c, list, count);
     else if (ns <= 2) cutcell_kernel<2><<<ng, TPB, 0, st>>>(c, list, count);
     else if (ns <= 4) cutcell_kernel<4><<<ng, TPB, 0, st>>>(c, list, count);

@@ -91,4 +91,10 @@ cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st);
 cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g, int s_src, double time,
                               cudaStream_t st);
 
+// Cut-cell cache (mfg_ib.cu): drop entries whose volume fraction changed
+// (after a host synchronization), free everything, switch on/off.
+void cutcache_sweep();
+void cutcache_release();
+void cutcache_enable(bool on);
+
 }  // namespace mfg
