@@ -190,7 +190,7 @@ def run_amr(a):
     cells = lib.mfg_boxlist_cells(h)
     dt = 1e-9
     res = {}
-    tune = (C.c_double * 15)()
+    tune = (C.c_double * 16)()
     for name, mode in (("plain_per_box", 0), ("batched", 1), ("batched_graph", 2)):
         if mode == 1:
             with torch.cuda.stream(s):
@@ -222,7 +222,8 @@ def run_amr(a):
            "speedup_batched_graph_vs_plain": res["plain_per_box"]["ms_per_step"] / res["batched_graph"]["ms_per_step"],
            "speedup_batched_vs_plain": res["plain_per_box"]["ms_per_step"] / res["batched"]["ms_per_step"],
            "autotune": {p: {"tile_items": tune[3 * i], "grid": tune[3 * i + 1], "ms": tune[3 * i + 2]}
-                        for i, p in enumerate(phases)}}
+                        for i, p in enumerate(phases)},
+           "flux_form": {2: "column sweep", 1: "WENO5 per face", 0: "generic"}.get(int(tune[15]), "?")}
     print(json.dumps(out))
     return 0
 

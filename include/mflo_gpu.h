@@ -336,8 +336,10 @@ int mfg_boxlist_destroy(mfg_boxlist* list);
 int mfg_boxlist_step(mfg_boxlist* list, double time, double dt, int mode, void* stream);
 
 /* Chooses tile size and grid size for each batched phase by timing candidates
- * (CUDA events) on this machine list; results (optional, 15 doubles): per phase
- * tile items, grid blocks, best ms.  Synchronizes. */
+ * (CUDA events) on this machine list, and for WENO5 the flux form (column sweep
+ * or per face, bitwise equal); results (optional, 16 doubles): per phase
+ * (fill, cut, face, flux, update) tile items, grid blocks, best ms, then the
+ * flux kernel (2 column sweep, 1 WENO5 per face, 0 generic).  Synchronizes. */
 int mfg_boxlist_autotune(mfg_boxlist* list, double dt, double* results, void* stream);
 
 /* Number of valid cells in the list. */

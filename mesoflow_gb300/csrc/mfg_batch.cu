@@ -229,6 +229,26 @@ __global__ void __launch_bounds__(BT) bk_flux(const RhsBox* __restrict__ B, cons
     TILE_END
 }
 
+constexpr int SWEEP_BT = 128;
+__global__ void __launch_bounds__(SWEEP_BT, 2) bk_flux_sweep(const RhsBox* __restrict__ B,
+                                                             const Tile* __restrict__ tiles, int ntiles) {
+    TILE_LOOP
+    flux5_sweep_body(B[tl.box], tl.part >> 5, tl.part & 31, t);
+    TILE_END
+}
+__global__ void __launch_bounds__(SWEEP_BT, 2) bk_flux5_face(const RhsBox* __restrict__ B,
+                                                             const Tile* __restrict__ tiles, int ntiles) {
+    TILE_LOOP
+    flux5_face_body(B[tl.box], tl.part >> 5, tl.part & 31, t);
+    TILE_END
+}
+
+// WENO5 with Navier-Stokes terms in the one-division mode: column sweep or
+// per-face form of the same arithmetic (bitwise equal; the autotuner picks).
+bool flux_sweep_mode() {
+    return c_host_params().order_hyp == 5 && c_host_params().do_ns && weno_fast_mode();
+}
+
 __global__ void __launch_bounds__(BT) bk_update(const RhsBox* __restrict__ B, const Tile* __restrict__ tiles,
                                                 int ntiles, int stage, double dt) {
     TILE_LOOP
@@ -318,12 +338,17 @@ struct mfg_boxlist {
     PhaseTiles ph[PH_COUNT];
     std::vector<PhaseTiles> level_grown;  // per-level tiles of grown cells (plain-mode fill)
     int cut_grid = 0;
+    int flux_form = 2;          // with flux_sweep_mode(): 2 column sweep, 1 per-face form
+    int flux_tiles_kind = -1;   // flux_kind() the flux tiles were built for
     cudaGraphExec_t gexec = nullptr;
     double gdt = 0.0;
     long long cells = 0;
 };
 
 namespace {
+
+// Flux-phase kernel: 0 flux_body, 1 WENO5 per-face form, 2 WENO5 column sweep.
+int flux_kind(const mfg_boxlist& L) { return flux_sweep_mode() ? L.flux_form : 0; }
 
 void free_tiles(PhaseTiles& p) {
     if (p.d) cudaFree(p.d);
@@ -342,6 +367,7 @@ long long items_of(const mfg_boxlist& L, int ph, int b, int part) {
         case PH_FACE: return (n[0] + (part == 0)) * (n[1] + (part == 1)) * (n[2] + (part == 2));
         case PH_FLUX: {
             const int d = part >> 5;
+            if (flux_kind(L) == 2) return sweep_items(L.rhs[b], d);
             return (n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
         }
     }
@@ -374,6 +400,7 @@ cudaError_t build_tiles(mfg_boxlist& L, PhaseTiles& P, int ph, int tile_items, i
         }
     }
     free_tiles(P);
+    if (ph == PH_FLUX) L.flux_tiles_kind = flux_kind(L);
     P.tile_items = tile_items;
     P.n = (int)t.size();
     P.grid = P.grid_cap > 0 ? std::min(P.n, P.grid_cap) : P.n;
@@ -433,7 +460,11 @@ void b_rhs(mfg_boxlist& L, int stage, double dt, cudaStream_t st) {
     if (!(c_host_params().do_ns && ord <= 2)) {
         const PhaseTiles& T = L.ph[PH_FLUX];
         ProfScope ps(K_FLUX, st);
-        if (weno_fast_mode())
+        if (flux_kind(L) == 2)
+            bk_flux_sweep<<<T.grid, SWEEP_BT, 0, st>>>(L.d_rhs, T.d, T.n);
+        else if (flux_kind(L) == 1)
+            bk_flux5_face<<<T.grid, SWEEP_BT, 0, st>>>(L.d_rhs, T.d, T.n);
+        else if (weno_fast_mode())
             bk_flux<true><<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n);
         else
             bk_flux<false><<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n);
@@ -685,6 +716,11 @@ int mfg_boxlist_step(mfg_boxlist* L, double time, double dt, int mode, void* str
     (void)time;
     if (!L) return MFG_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    if (L->flux_tiles_kind != flux_kind(*L)) {  // the WENO mode changed since the tiles were built
+        drop_graph(*L);
+        if (build_tiles(*L, L->ph[PH_FLUX], PH_FLUX, L->ph[PH_FLUX].tile_items, -1) != cudaSuccess)
+            return MFG_ERR_CUDA;
+    }
     if (mode == 0) return step_plain(*L, dt, st);
     if (mode == 1) {
         step_batched(*L, dt, st);
@@ -727,9 +763,12 @@ int mfg_boxlist_autotune(mfg_boxlist* L, double dt, double* results, void* strea
     for (int p = 0; p < PH_COUNT; ++p) {
         if (p == PH_FLUX && c_host_params().do_ns && ord <= 2) continue;
         float best = 1e30f;
-        int bt = L->ph[p].tile_items, bg = L->ph[p].grid_cap;
+        int bt = L->ph[p].tile_items, bg = L->ph[p].grid_cap, bf = L->flux_form;
+        const int nforms = (p == PH_FLUX && flux_sweep_mode()) ? 2 : 1;
+        for (int form = 0; form < nforms; ++form)
         for (int ti : tiles_c)
             for (int gc : grids_c) {
+                if (nforms == 2) L->flux_form = 2 - form;
                 PhaseTiles& P = L->ph[p];
                 P.grid_cap = gc ? gc * sms : 0;
                 if (build_tiles(*L, P, p, ti, -1) != cudaSuccess) return MFG_ERR_CUDA;
@@ -743,7 +782,14 @@ int mfg_boxlist_autotune(mfg_boxlist* L, double dt, double* results, void* strea
                             NS_DISPATCH(bk_face, (P.grid, BT, 0, st), (L->d_rhs, P.d, P.n));
                             break;
                         }
-                        case PH_FLUX: bk_flux<true><<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n); break;
+                        case PH_FLUX:
+                            if (flux_kind(*L) == 2)
+                                bk_flux_sweep<<<P.grid, SWEEP_BT, 0, st>>>(L->d_rhs, P.d, P.n);
+                            else if (flux_kind(*L) == 1)
+                                bk_flux5_face<<<P.grid, SWEEP_BT, 0, st>>>(L->d_rhs, P.d, P.n);
+                            else
+                                bk_flux<true><<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n);
+                            break;
                         case PH_UPDATE: bk_update<<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n, 0, dt); break;
                     }
                     cudaEventRecord(e1, st);
@@ -756,14 +802,17 @@ int mfg_boxlist_autotune(mfg_boxlist* L, double dt, double* results, void* strea
                     best = ms_min;
                     bt = ti;
                     bg = P.grid_cap;
+                    bf = L->flux_form;
                 }
             }
+        L->flux_form = bf;
         L->ph[p].grid_cap = bg;
         if (build_tiles(*L, L->ph[p], p, bt, -1) != cudaSuccess) return MFG_ERR_CUDA;
         if (results) {
             results[3 * p + 0] = bt;
             results[3 * p + 1] = L->ph[p].grid;
             results[3 * p + 2] = best;
+            if (p == PH_FLUX) results[3 * PH_COUNT] = flux_kind(*L);
         }
     }
     cudaEventDestroy(e0);

@@ -12,6 +12,10 @@
 //                 component (WENO5-JS / MUSCL+AUSM+-up / central), species
 //                 diffusion, and the viscous terms, written once per face and
 //                 read by both neighbouring cells.
+//   flux5_sweep_kernel  WENO5 with Navier-Stokes terms in the one-division
+//                 mode: per (column segment along d, component), the per-cell
+//                 parts of the reconstruction computed once per cell and kept
+//                 in registers while the thread walks the faces.
 //   update_kernel per (cell, component): flux divergence, IB masking, NaN
 //                 status, and the RK3 stage algebra.
 // Semantics: compute_flux (Source/Src_3d/compute_flux_3d.H:88-430),
@@ -43,6 +47,16 @@ template <bool FAST>
 __global__ void __launch_bounds__(TPB) flux_kernel(RhsBox B, int d) {
     flux_body<FAST>(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
+constexpr int SWEEP_TPB = 128;
+__global__ void __launch_bounds__(SWEEP_TPB, 2) flux5_sweep_kernel(RhsBox B, int d) {
+    flux5_sweep_body(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(SWEEP_TPB, 2) flux5_face_kernel(RhsBox B, int d) {
+    flux5_face_body(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+// Column segments of one box fill the GPU only for large boxes; smaller
+// launches use the per-face form of the same arithmetic.
+constexpr int64_t SWEEP_MIN_THREADS = 152 * 2 * SWEEP_TPB * 2;
 __global__ void __launch_bounds__(TPB) update_kernel(RhsBox B, int stage, double dt) {
     update_body(B, stage, dt, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -72,8 +86,19 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
             face_kernel<NS><<<blocks_for(nf), TPB, 0, st>>>(B, d);
         }
         if (c_host_params().do_ns && ord <= 2) continue;  // the face kernel wrote the fluxes
-        dim3 g(blocks_for(nf), C);
         ProfScope ps(K_FLUX, st);
+        if (fast && ord == 5 && c_host_params().do_ns) {
+            const int64_t ns = sweep_items(B, d);
+            if (ns * C >= SWEEP_MIN_THREADS) {
+                dim3 g((unsigned)((ns + SWEEP_TPB - 1) / SWEEP_TPB), C);
+                flux5_sweep_kernel<<<g, SWEEP_TPB, 0, st>>>(B, d);
+            } else {
+                dim3 g((unsigned)((nf + SWEEP_TPB - 1) / SWEEP_TPB), C);
+                flux5_face_kernel<<<g, SWEEP_TPB, 0, st>>>(B, d);
+            }
+            continue;
+        }
+        dim3 g(blocks_for(nf), C);
         if (fast)
             flux_kernel<true><<<g, TPB, 0, st>>>(B, d);
         else

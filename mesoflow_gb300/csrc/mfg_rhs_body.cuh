@@ -538,6 +538,283 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
 }
 
 
+// ---------------------------------------------------------------------------
+// WENO5 column sweep (order 5 with Navier-Stokes terms, one-division mode):
+// one thread walks a segment of faces along d for one component, keeping the
+// per-cell parts of the reconstruction in registers.
+//
+// The six smoothness indicators and six candidate polynomials of a face's two
+// WENO5-JS edges (flux_schemes.H:373-446) are functions of the three cells
+// centred on f-2, f-1, f, f+1; per centre y with neighbours (x, y, z) there
+// are three distinct indicators, K1 t^2 + A with t = x - 2y + z and
+// A = (3x-4y+z)^2/4, (x-4y+3z)^2/4 or (x-z)^2/4, and four distinct
+// polynomials.  Computing them once per cell instead of once per face use
+// (six uses) and rebuilding each cell's Euler flux once instead of six times
+// removes most of the per-face FP64 work; each face then only combines the
+// nonlinear weights.  The left edge uses (B, C, A) at centres (f-2, f-1, f),
+// the right edge (A, C, B) at (f+1, f, f-1).  Results differ from the
+// per-face form by rounding only (the mirrored edge evaluates the same
+// polynomials with operands in the other order).
+// ---------------------------------------------------------------------------
+constexpr int SWEEP_SEG = 32;  // longest face segment per thread
+
+struct WenoCell {
+    double bA, bB, bC, p1, p2, p3, p4;
+};
+
+// The sweep and the per-face form must round identically, so every operation
+// of the per-cell and per-face parts is an explicit intrinsic (the compiler
+// may neither contract nor reorder them differently in the two contexts).
+__device__ __forceinline__ WenoCell weno_cell(double x, double y, double z) {
+    WenoCell r;
+    const double t = __dadd_rn(__fma_rn(-2.0, y, x), z);
+    const double kt = __dmul_rn(13.0 / 12.0, __dmul_rn(t, t));
+    const double tA = __dadd_rn(__fma_rn(-4.0, y, __dmul_rn(3.0, x)), z);
+    const double tB = __fma_rn(3.0, z, __fma_rn(-4.0, y, x));
+    const double q = __dsub_rn(x, z);
+    r.bA = __fma_rn(__dmul_rn(0.25, tA), tA, kt);
+    r.bB = __fma_rn(__dmul_rn(0.25, tB), tB, kt);
+    r.bC = __fma_rn(__dmul_rn(0.25, q), q, kt);
+    r.p1 = __fma_rn(11.0, z, __fma_rn(-7.0, y, __dmul_rn(2.0, x)));
+    r.p2 = __fma_rn(2.0, z, __fma_rn(5.0, y, -x));
+    r.p3 = __dsub_rn(__fma_rn(5.0, y, __dmul_rn(2.0, x)), z);
+    r.p4 = __fma_rn(2.0, z, __fma_rn(-7.0, y, __dmul_rn(11.0, x)));
+    return r;
+}
+
+// Nonlinear combination of one edge: indicators b2, b1, b0 with linear
+// weights 1, 6, 3 and candidates v2, v1, v0 (divided by 6).  The weight sum
+// is a positive normal number, so a Newton-refined reciprocal replaces the
+// division.
+__device__ __forceinline__ double weno_comb(double b2, double b1, double b0, double v2, double v1, double v0) {
+    const double s2 = __dadd_rn(kEpsWeno, b2), s1 = __dadd_rn(kEpsWeno, b1), s0 = __dadd_rn(kEpsWeno, b0);
+    const double d2 = __dmul_rn(s2, s2), d1 = __dmul_rn(s1, s1), d0 = __dmul_rn(s0, s0);
+    const double e2 = __dmul_rn(d1, d0), e1 = __dmul_rn(6.0, __dmul_rn(d2, d0)), e0 = __dmul_rn(3.0, __dmul_rn(d2, d1));
+    const double num = __fma_rn(e0, v0, __fma_rn(e1, v1, __dmul_rn(e2, v2)));
+    const double den = __dadd_rn(__dadd_rn(e2, e1), e0);
+    return __dmul_rn(num, rcp_pos(__dmul_rn(6.0, den)));
+}
+
+// Transverse directions of a sweep along d (the first one is x when d != 0,
+// so consecutive threads read consecutive addresses).
+__host__ __device__ __forceinline__ void sweep_dirs(int d, int& a, int& b) {
+    a = (d == 0) ? 1 : 0;
+    b = (d == 2) ? 1 : 2;
+}
+
+__host__ __device__ __forceinline__ int sweep_nseg(const RhsBox& B, int d) {
+    const int nf = B.hi[d] - B.lo[d] + 2;
+    return (nf + SWEEP_SEG - 1) / SWEEP_SEG;
+}
+
+__host__ __device__ __forceinline__ int64_t sweep_items(const RhsBox& B, int d) {
+    int a, b;
+    sweep_dirs(d, a, b);
+    return (int64_t)(B.hi[a] - B.lo[a] + 1) * (B.hi[b] - B.lo[b] + 1) * sweep_nseg(B, d);
+}
+
+// Raw values of one cell for component c: the state and its Euler flux along d.
+__device__ __forceinline__ void sweep_raw(const RhsBox& B, int d, int c, int sc, int64_t os, int64_t ox, double& u,
+                                          double& f) {
+    const Fab& S = B.sb;
+    const Fab& X = B.aux;
+    u = S.p[os + sc * S.ns];
+    const double va = (c >= 1 && c <= 3) ? X.p[ox + (AUX_VX + c - 1) * X.ns] : 0.0;
+    f = euler_flux(c, d, u, S.p[os + RHO * S.ns], va, X.p[ox + (AUX_VX + d) * X.ns], X.p[ox + AUX_PF * X.ns],
+                   S.p[os + RHOE * S.ns]);
+}
+
+// First-order stencil near the immersed boundary (compute_flux_3d.H:233-249):
+// the six cells collapse to (L, L, L, R, R, R).  Both edges then have the
+// indicators 0, (K1 + 1/4) D^2 and (K1 + 9/4) D^2 with D = R - L, hence the
+// same nonlinear weights, and the candidates 6L, 4L + 2R, 2L + 4R (left edge)
+// and their mirror images (right edge).
+__device__ __forceinline__ void weno_collapsed(double L, double R, double& up, double& um) {
+    const double D = __dsub_rn(R, L), D2 = __dmul_rn(D, D);
+    const double s2 = kEpsWeno, s1 = __fma_rn(13.0 / 12.0 + 0.25, D2, kEpsWeno),
+                 s0 = __fma_rn(13.0 / 12.0 + 2.25, D2, kEpsWeno);
+    const double d2 = __dmul_rn(s2, s2), d1 = __dmul_rn(s1, s1), d0 = __dmul_rn(s0, s0);
+    const double e2 = __dmul_rn(d1, d0), e1 = __dmul_rn(6.0, __dmul_rn(d2, d0)), e0 = __dmul_rn(3.0, __dmul_rn(d2, d1));
+    const double r = rcp_pos(__dmul_rn(6.0, __dadd_rn(__dadd_rn(e2, e1), e0)));
+    const double vl1 = __fma_rn(2.0, R, __dmul_rn(4.0, L)), vl0 = __fma_rn(4.0, R, __dmul_rn(2.0, L));
+    const double vr1 = __fma_rn(2.0, L, __dmul_rn(4.0, R)), vr0 = __fma_rn(4.0, L, __dmul_rn(2.0, R));
+    up = __dmul_rn(__fma_rn(e0, vl0, __fma_rn(e1, vl1, __dmul_rn(e2, __dmul_rn(6.0, L)))), r);
+    um = __dmul_rn(__fma_rn(e0, vr0, __fma_rn(e1, vr1, __dmul_rn(e2, __dmul_rn(6.0, R)))), r);
+}
+
+// The four cells of a face's stencil (centres f-2 .. f+1) for the state and
+// for the Euler flux of one component.
+struct WenoWindow {
+    WenoCell u0, u1, u2, u3, f0, f1, f2, f3;
+};
+
+// Flux of component c through one face (the sweep and the per-face form share
+// it, so they agree bitwise): uL/uR and fL/fR are the state and Euler flux of
+// the two cells next to the face, vfL/vfR their volume fractions.
+__device__ __forceinline__ double flux5_face(const RhsBox& B, int d, int c, const Fab& FS, int64_t qf,
+                                             const WenoWindow& w, double uL, double uR, double fL, double fR,
+                                             double vfL, double vfR) {
+    const DevParams& P = c_P;
+    const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
+    double F = 0.0;
+    if (flags & 1) {
+        const double lam = FS.p[qf + FS_LAMBDA * FS.ns];
+        double fp, fm, up, um;
+        if (!(flags & 2)) {
+            fp = weno_comb(w.f0.bB, w.f1.bC, w.f2.bA, w.f0.p1, w.f1.p2, w.f2.p3);
+            fm = weno_comb(w.f3.bA, w.f2.bC, w.f1.bB, w.f3.p4, w.f2.p3, w.f1.p2);
+            up = weno_comb(w.u0.bB, w.u1.bC, w.u2.bA, w.u0.p1, w.u1.p2, w.u2.p3);
+            um = weno_comb(w.u3.bA, w.u2.bC, w.u1.bB, w.u3.p4, w.u2.p3, w.u1.p2);
+        } else {
+            weno_collapsed(fL, fR, fp, fm);
+            weno_collapsed(uL, uR, up, um);
+        }
+        const double fh = __fma_rn(0.5, __fma_rn(lam, up, fp), __dmul_rn(0.5, __fma_rn(-lam, um, fm)));
+        F = (c < NCONS) ? fh : __dmul_rn(P.advect_flag[c - NCONS], fh);
+        if (c >= RHOU && c <= RHOW) F = __dsub_rn(F, FS.p[qf + (FS_VIS + c - 1) * FS.ns]);
+        if (c == RHOE) {
+            F = __dsub_rn(F, FS.p[qf + (FS_VISE + 0) * FS.ns]);
+            F = __dsub_rn(F, FS.p[qf + (FS_VISE + 1) * FS.ns]);
+            F = __dsub_rn(F, FS.p[qf + (FS_VISE + 2) * FS.ns]);
+        }
+    }
+    if (c == RHOE) F = __dsub_rn(F, FS.p[qf + FS_THERM * FS.ns]);
+    if (c >= NCONS) {  // species diffusion (compute_flux_3d.H:425-428)
+        const int s = c - NCONS;
+        double Dh = P.diff_hm[s];
+        if (P.diff_mode[s] != MFG_TRANSPORT_CONST) {  // harmonic mean of gas vf + solid (1 - vf)
+            const double g = P.diff_gas[s], so = P.diff_solid[s];
+            const double dl = __fma_rn(g, vfL, __dmul_rn(so, __dsub_rn(1.0, vfL)));
+            const double dr = __fma_rn(g, vfR, __dmul_rn(so, __dsub_rn(1.0, vfR)));
+            Dh = __ddiv_rn(__dmul_rn(__dmul_rn(2.0, dl), dr), __dadd_rn(__dadd_rn(dl, dr), 1e-30));
+        }
+        F = __fma_rn(-__dmul_rn(Dh, __dsub_rn(uR, uL)), B.idx[d], F);
+    }
+    return F;
+}
+
+__device__ __forceinline__ void flux5_store(const RhsBox& B, int d, int c, int sc, const Idx3& f, double F) {
+    const Fab& O = B.flx[d];
+    O.p[O.off(f.i, f.j, f.k) + c * O.ns] = F;
+    if (B.uflux[d].p) {
+        const Fab& U = B.uflux[d];
+        const int64_t qu = U.off(f.i, f.j, f.k);
+        U.p[qu + sc * U.ns] = F;
+        if (c == 0)
+            for (int z = NCONS; z < NFLO; ++z) U.p[qu + z * U.ns] = 0.0;
+    }
+}
+
+// Per-face form (for launches too small to fill the GPU with column
+// segments): one thread per (face, component) builds the four cells itself.
+__device__ __forceinline__ void flux5_face_body(const RhsBox& B, int d, int c, int64_t t) {
+    int len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    if (t >= (int64_t)len[0] * len[1] * len[2]) return;
+    const Idx3 f = delinear(t, B.lo, len);
+    const Fab& S = B.sb;
+    const Fab& X = B.aux;
+    const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int64_t xd = (d == 0) ? 1 : (d == 1) ? X.js : X.ks;
+    const int64_t oR = S.off(f.i, f.j, f.k), xR = X.off(f.i, f.j, f.k);
+    double ru[6], rf[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) sweep_raw(B, d, c, sc, oR + (q - 3) * sd, xR + (q - 3) * xd, ru[q], rf[q]);
+    WenoWindow w;
+    w.u0 = weno_cell(ru[0], ru[1], ru[2]);
+    w.u1 = weno_cell(ru[1], ru[2], ru[3]);
+    w.u2 = weno_cell(ru[2], ru[3], ru[4]);
+    w.u3 = weno_cell(ru[3], ru[4], ru[5]);
+    w.f0 = weno_cell(rf[0], rf[1], rf[2]);
+    w.f1 = weno_cell(rf[1], rf[2], rf[3]);
+    w.f2 = weno_cell(rf[2], rf[3], rf[4]);
+    w.f3 = weno_cell(rf[3], rf[4], rf[5]);
+    const double* vfp = S.p + VFRAC * S.ns;
+    const Fab& FS = B.fs[d];
+    const double F = flux5_face(B, d, c, FS, FS.off(f.i, f.j, f.k), w, ru[2], ru[3], rf[2], rf[3], vfp[oR - sd],
+                                vfp[oR]);
+    flux5_store(B, d, c, sc, f, F);
+}
+
+__device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, int64_t t) {
+    if (t >= sweep_items(B, d)) return;
+    int ta, tb;
+    sweep_dirs(d, ta, tb);
+    const int na = B.hi[ta] - B.lo[ta] + 1, nb = B.hi[tb] - B.lo[tb] + 1;
+    const int64_t ncol = (int64_t)na * nb;
+    const int seg = (int)(t / ncol);
+    const int64_t col = t - (int64_t)seg * ncol;
+    const int nf = B.hi[d] - B.lo[d] + 2;
+    const int nseg = sweep_nseg(B, d);
+    const int per = (nf + nseg - 1) / nseg;
+    const int f0 = B.lo[d] + seg * per;
+    const int f1 = min(B.lo[d] + nf - 1, f0 + per - 1);
+    if (f0 > f1) return;
+    int iv[3];
+    iv[ta] = B.lo[ta] + (int)(col % na);
+    iv[tb] = B.lo[tb] + (int)(col / na);
+    iv[d] = f0;
+    const Fab& S = B.sb;
+    const Fab& X = B.aux;
+    const Fab& FS = B.fs[d];
+    const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int64_t xd = (d == 0) ? 1 : (d == 1) ? X.js : X.ks;
+    const int64_t fd = (d == 0) ? 1 : (d == 1) ? FS.js : FS.ks;
+    int64_t oR = S.off(iv[0], iv[1], iv[2]);  // right cell of the current face
+    int64_t xR = X.off(iv[0], iv[1], iv[2]);
+    int64_t qf = FS.off(iv[0], iv[1], iv[2]);
+    // raw values of cells f-3 .. f+2
+    double ru[6], rf[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) sweep_raw(B, d, c, sc, oR + (q - 3) * sd, xR + (q - 3) * xd, ru[q], rf[q]);
+    WenoWindow w;
+    w.u0 = weno_cell(ru[0], ru[1], ru[2]);
+    w.u1 = weno_cell(ru[1], ru[2], ru[3]);
+    w.u2 = weno_cell(ru[2], ru[3], ru[4]);
+    w.u3 = weno_cell(ru[3], ru[4], ru[5]);
+    w.f0 = weno_cell(rf[0], rf[1], rf[2]);
+    w.f1 = weno_cell(rf[1], rf[2], rf[3]);
+    w.f2 = weno_cell(rf[2], rf[3], rf[4]);
+    w.f3 = weno_cell(rf[3], rf[4], rf[5]);
+    double uL = ru[2], uR = ru[3], uP1 = ru[4], uP2 = ru[5];
+    double fL = rf[2], fR = rf[3], fP1 = rf[4], fP2 = rf[5];
+    const double* vfp = S.p + VFRAC * S.ns;
+    for (int f = f0;; ++f) {
+        const double F = flux5_face(B, d, c, FS, qf, w, uL, uR, fL, fR, vfp[oR - sd], vfp[oR]);
+        Idx3 fi;
+        fi.i = iv[0];
+        fi.j = iv[1];
+        fi.k = iv[2];
+        flux5_store(B, d, c, sc, fi, F);
+        if (f == f1) break;
+        // advance one face: load cell f+3, build the cell centred on f+2
+        ++iv[d];
+        oR += sd;
+        xR += xd;
+        qf += fd;
+        double un, fn;
+        sweep_raw(B, d, c, sc, oR + 2 * sd, xR + 2 * xd, un, fn);
+        w.u0 = w.u1;
+        w.u1 = w.u2;
+        w.u2 = w.u3;
+        w.u3 = weno_cell(uP1, uP2, un);
+        w.f0 = w.f1;
+        w.f1 = w.f2;
+        w.f2 = w.f3;
+        w.f3 = weno_cell(fP1, fP2, fn);
+        uL = uR;
+        uR = uP1;
+        uP1 = uP2;
+        uP2 = un;
+        fL = fR;
+        fR = fP1;
+        fP1 = fP2;
+        fP2 = fn;
+    }
+}
+
 // Work items of each phase for one box.
 __host__ __device__ __forceinline__ int64_t prim_items(const RhsBox& B) {
     return (int64_t)(B.hi[0] - B.lo[0] + 7) * (B.hi[1] - B.lo[1] + 7) * (B.hi[2] - B.lo[2] + 7);

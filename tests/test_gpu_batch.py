@@ -81,7 +81,7 @@ def test_autotune_keeps_results():
         ml = MultiLevel(amr, backend="torch", device="cuda")
         h = _boxlist(lib, ml.descriptors(), len(amr.boxes), ml.geoms(), len(amr.geoms))
         if tune:
-            r = (C.c_double * 15)()
+            r = (C.c_double * 16)()
             with torch.cuda.stream(s):
                 abi.check("mfg_boxlist_autotune", lib.mfg_boxlist_autotune(h, dt, r, st))
             assert all(r[3 * p + 1] >= 1 for p in (0, 1, 2, 4))
