@@ -15,16 +15,19 @@
 // so no lane idles on pure fluid or solid cells.
 //
 // Cut-cell cache: the list and the weights depend on the volume fraction of
-// the grown box only, which the solver never changes, while the reference
-// recomputes them for every stage of every step.  The first call for a box
-// (keyed by its Sborder view and extent) keeps a copy of the grown volume
-// fraction, the list, and every cut cell's fluid-neighbour mask and weights.
-// Every later call first compares the volume fraction with the copy on the
-// device (exact, bit patterns); the cut-cell kernel uses the stored weights
-// when nothing changed and recomputes everything on the fly otherwise, so a
-// changed geometry is never served stale weights.  Both paths give bitwise
-// equal results.  Changed boxes are dropped from the cache by
-// cutcache_sweep (called where the host synchronizes anyway).
+// the grown box only, while the reference recomputes them for every stage of
+// every step.  The volume fraction is a state component, so the RK3 algebra
+// can move it by an ulp (x 1/3 in stage 3), but the geometry does not change.
+// The first call for a box (keyed by its Sborder view and extent) keeps a
+// copy of the grown volume fraction, the list, and every cut cell's
+// fluid-neighbour mask and weights.  Every later call first compares the
+// volume fraction with the copy on the device (exact, bit patterns): the
+// cut-cell kernel uses the stored weights when nothing changed; otherwise it
+// rebuilds the list, recomputes, and (when the new list fits the entry)
+// stores the new weights and volume fraction on the device, so a changed
+// geometry is never served stale weights and no host round trip is needed.
+// All paths give bitwise equal results.  Entries whose new list did not fit
+// are dropped by cutcache_sweep (called where the host synchronizes anyway).
 #include <algorithm>
 #include <unordered_map>
 #include <vector>
@@ -111,21 +114,62 @@ __global__ void cut_weights_kernel(CutBox c, const int* __restrict__ list, unsig
     cut_weights_one(c, list[w], (int)w, mask, scal, wn);
 }
 
-// Stored weights when the volume fraction is unchanged (*dirty == 0), else the
-// on-the-fly form over the freshly built list.
+// Stored weights when the volume fraction is unchanged (*dirty == 0).  Else
+// the freshly built list is processed: when it fits the entry's capacity,
+// each cut cell's weights are stored first (the cache is refreshed on the
+// device, no host round trip) and then applied; otherwise the on-the-fly form
+// runs.  Either way the results are those of the on-the-fly form, bitwise.
 template <int NS>
-__global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, const int* __restrict__ clist, unsigned ncut,
-                                                             CutCacheView cc, const unsigned* __restrict__ dirty,
+__global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, int* __restrict__ clist,
+                                                             const unsigned* __restrict__ ncut, unsigned cap,
+                                                             unsigned long long* mask, double* scal, double* wn,
+                                                             const unsigned* __restrict__ dirty,
                                                              const int* __restrict__ list,
                                                              const unsigned* __restrict__ count) {
+    const CutCacheView cc = {mask, scal, wn};
     if (*dirty) {
         const unsigned n = *count;
-        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
-            cutcell_one<NS>(c, list[w]);
+        const bool refresh = n <= cap;
+        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+            const int t = list[w];
+            if (refresh) {
+                clist[w] = t;
+                cut_weights_one(c, t, (int)w, mask, scal, wn);
+                cutcell_cached<NS>(c, t, (int)w, cc);
+            } else {
+                cutcell_one<NS>(c, t);
+            }
+        }
         return;
     }
-    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ncut; w += gridDim.x * blockDim.x)
+    const unsigned n = *ncut;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
         cutcell_cached<NS>(c, clist[w], (int)w, cc);
+}
+
+// After a refresh: the stored volume fraction and count follow the new
+// geometry and the entry is clean again.  Every block reads *dirty before it
+// counts itself done in ncut[1]; the last block clears the flag.
+__global__ void cut_commit_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int l1, int l2, double* __restrict__ vf,
+                                  unsigned* __restrict__ dirty, const unsigned* __restrict__ count, unsigned cap,
+                                  unsigned* __restrict__ ncut) {
+    if (!*dirty || *count > cap) return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < (int64_t)l0 * l1 * l2) {
+        const int64_t a = t / l0;
+        vf[t] = S(lo0 + (int)(t - a * l0), lo1 + (int)(a % l1), lo2 + (int)(a / l1), VFRAC);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(ncut + 1, 1u);
+        if (done == gridDim.x - 1) {
+            ncut[0] = *count;
+            ncut[1] = 0;
+            __threadfence();
+            *dirty = 0;
+        }
+    }
 }
 
 double g_wdir_dx[3] = {-1.0, -1.0, -1.0};
@@ -136,7 +180,8 @@ struct CutEntry {
     double dx[3];
     double* vf = nullptr;
     int* list = nullptr;
-    unsigned ncut = 0;
+    unsigned ncut = 0;            // cut cells when built (capacity of the weight arrays)
+    unsigned* ncut_d = nullptr;   // [current count, commit counter]
     unsigned long long* mask = nullptr;
     double* scal = nullptr;
     double* wn = nullptr;
@@ -156,6 +201,7 @@ struct CutCache {
 void free_entry(CutEntry& e) {
     cudaFree(e.vf);
     cudaFree(e.list);
+    cudaFree(e.ncut_d);
     cudaFree(e.mask);
     cudaFree(e.scal);
     cudaFree(e.wn);
@@ -220,6 +266,11 @@ bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry&
     if (cudaMalloc(&e.scal, n * 2 * sizeof(double)) != cudaSuccess) return false;
     if (cudaMalloc(&e.wn, n * CUT_SLOTS * sizeof(double)) != cudaSuccess) return false;
     if ((e.slot = new_slot(st)) < 0) return false;
+    if (cudaMalloc(&e.ncut_d, 2 * sizeof(unsigned)) != cudaSuccess) return false;
+    const unsigned hc[2] = {e.ncut, 0u};
+    if (cudaMemcpyAsync(e.ncut_d, hc, sizeof(hc), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return false;
     if (e.ncut)
         cut_weights_kernel<<<(e.ncut + TPB - 1) / TPB, TPB, 0, st>>>(c, e.list, e.ncut, e.mask, e.scal, e.wn);
     g_cache.bytes += ng * sizeof(double) + c.n * sizeof(int) + need;
@@ -322,13 +373,18 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
         cut_vf_kernel<<<(unsigned)((ngc + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0,
                                                                       l1, l2, ce->vf, dirty, 1);
         cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, dirty);
-        const CutCacheView cv = {ce->mask, ce->scal, ce->wn};
         const unsigned ng = (unsigned)std::min<int64_t>(std::max<int64_t>(nb, 1), 152 * 8);
-        if (ns <= 1) cutcell_cached_kernel<1><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
-        else if (ns <= 2) cutcell_cached_kernel<2><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
-        else if (ns <= 4) cutcell_cached_kernel<4><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
-        else if (ns <= 8) cutcell_cached_kernel<8><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
-        else cutcell_cached_kernel<16><<<ng, TPB, 0, st>>>(c, ce->list, ce->ncut, cv, dirty, list, count);
+        const unsigned cap = ce->ncut;
+#define MFG_CUT_ARGS c, ce->list, ce->ncut_d, cap, ce->mask, ce->scal, ce->wn, dirty, list, count
+        if (ns <= 1) cutcell_cached_kernel<1><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
+        else if (ns <= 2) cutcell_cached_kernel<2><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
+        else if (ns <= 4) cutcell_cached_kernel<4><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
+        else if (ns <= 8) cutcell_cached_kernel<8><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
+        else cutcell_cached_kernel<16><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
+#undef MFG_CUT_ARGS
+        cut_commit_kernel<<<(unsigned)((ngc + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0,
+                                                                          l1, l2, ce->vf, dirty, count, cap,
+                                                                          ce->ncut_d);
         return cudaGetLastError();
     }
     cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, nullptr);

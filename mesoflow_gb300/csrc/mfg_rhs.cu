@@ -48,14 +48,15 @@ __global__ void __launch_bounds__(TPB) flux_kernel(RhsBox B, int d) {
     flux_body<FAST>(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 constexpr int SWEEP_TPB = 128;
-__global__ void __launch_bounds__(SWEEP_TPB, 2) flux5_sweep_kernel(RhsBox B, int d) {
-    flux5_sweep_body(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(SWEEP_TPB, 2) flux5_sweep_kernel(RhsBox B, int d, int seg) {
+    flux5_sweep_body(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, seg);
 }
 __global__ void __launch_bounds__(SWEEP_TPB, 2) flux5_face_kernel(RhsBox B, int d) {
     flux5_face_body(B, d, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
-// Column segments of one box fill the GPU only for large boxes; smaller
-// launches use the per-face form of the same arithmetic.
+// One box's column segments must fill the GPU: segments of 32, 16 or 8 faces
+// (longer ones share more per-cell work), else the per-face form of the same
+// arithmetic.
 constexpr int64_t SWEEP_MIN_THREADS = 152 * 2 * SWEEP_TPB * 2;
 __global__ void __launch_bounds__(TPB) update_kernel(RhsBox B, int stage, double dt) {
     update_body(B, stage, dt, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
@@ -88,10 +89,12 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
         if (c_host_params().do_ns && ord <= 2) continue;  // the face kernel wrote the fluxes
         ProfScope ps(K_FLUX, st);
         if (fast && ord == 5 && c_host_params().do_ns) {
-            const int64_t ns = sweep_items(B, d);
+            int seg = 32;
+            while (seg > 8 && sweep_items(B, d, seg) * C < SWEEP_MIN_THREADS) seg /= 2;
+            const int64_t ns = sweep_items(B, d, seg);
             if (ns * C >= SWEEP_MIN_THREADS) {
                 dim3 g((unsigned)((ns + SWEEP_TPB - 1) / SWEEP_TPB), C);
-                flux5_sweep_kernel<<<g, SWEEP_TPB, 0, st>>>(B, d);
+                flux5_sweep_kernel<<<g, SWEEP_TPB, 0, st>>>(B, d, seg);
             } else {
                 dim3 g((unsigned)((nf + SWEEP_TPB - 1) / SWEEP_TPB), C);
                 flux5_face_kernel<<<g, SWEEP_TPB, 0, st>>>(B, d);

@@ -556,7 +556,7 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
 // per-face form by rounding only (the mirrored edge evaluates the same
 // polynomials with operands in the other order).
 // ---------------------------------------------------------------------------
-constexpr int SWEEP_SEG = 32;  // longest face segment per thread
+constexpr int SWEEP_SEG = 32;  // longest face segment per thread (batched launches)
 
 struct WenoCell {
     double bA, bB, bC, p1, p2, p3, p4;
@@ -602,15 +602,15 @@ __host__ __device__ __forceinline__ void sweep_dirs(int d, int& a, int& b) {
     b = (d == 2) ? 1 : 2;
 }
 
-__host__ __device__ __forceinline__ int sweep_nseg(const RhsBox& B, int d) {
+__host__ __device__ __forceinline__ int sweep_nseg(const RhsBox& B, int d, int seg) {
     const int nf = B.hi[d] - B.lo[d] + 2;
-    return (nf + SWEEP_SEG - 1) / SWEEP_SEG;
+    return (nf + seg - 1) / seg;
 }
 
-__host__ __device__ __forceinline__ int64_t sweep_items(const RhsBox& B, int d) {
+__host__ __device__ __forceinline__ int64_t sweep_items(const RhsBox& B, int d, int seg = SWEEP_SEG) {
     int a, b;
     sweep_dirs(d, a, b);
-    return (int64_t)(B.hi[a] - B.lo[a] + 1) * (B.hi[b] - B.lo[b] + 1) * sweep_nseg(B, d);
+    return (int64_t)(B.hi[a] - B.lo[a] + 1) * (B.hi[b] - B.lo[b] + 1) * sweep_nseg(B, d, seg);
 }
 
 // Raw values of one cell for component c: the state and its Euler flux along d.
@@ -737,8 +737,8 @@ __device__ __forceinline__ void flux5_face_body(const RhsBox& B, int d, int c, i
     flux5_store(B, d, c, sc, f, F);
 }
 
-__device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, int64_t t) {
-    if (t >= sweep_items(B, d)) return;
+__device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, int64_t t, int seglen = SWEEP_SEG) {
+    if (t >= sweep_items(B, d, seglen)) return;
     int ta, tb;
     sweep_dirs(d, ta, tb);
     const int na = B.hi[ta] - B.lo[ta] + 1, nb = B.hi[tb] - B.lo[tb] + 1;
@@ -746,7 +746,7 @@ __device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, 
     const int seg = (int)(t / ncol);
     const int64_t col = t - (int64_t)seg * ncol;
     const int nf = B.hi[d] - B.lo[d] + 2;
-    const int nseg = sweep_nseg(B, d);
+    const int nseg = sweep_nseg(B, d, seglen);
     const int per = (nf + nseg - 1) / nseg;
     const int f0 = B.lo[d] + seg * per;
     const int f1 = min(B.lo[d] + nf - 1, f0 + per - 1);
