@@ -1,0 +1,104 @@
+"""Full-size checks of the GPU path on the benchmark configurations, through
+properties that do not need the oracle to finish a 256^3 run:
+
+* Sod 256 x 4 x 4, WENO5, CFL 0.5, 200 steps (the reference's ShockTube_N2
+  case): the GPU run equals the oracle's run of the same dt sequence in L2
+  (1e-10 relative) and its density profile stays within the smearing of the
+  exact Riemann solution (L1 < 0.004 at the final time; the oracle gives
+  0.0029).
+* 256^3 periodic 5-species Taylor-Green, WENO5: total mass, momentum, energy
+  and species mass are conserved to 1e-12 of the summed magnitudes over two
+  steps (the face fluxes telescope on a periodic box).
+* 256^3 immersed boundary, order 2: the per-box step with and without the
+  cut-cell cache and the batched step give bitwise equal states.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mesoflow_gb300 import abi, cases
+from mesoflow_gb300.driver import Mflo
+from mesoflow_gb300.level import Level
+from oracle_run import OracleLevel
+import riemann
+
+torch = pytest.importorskip("torch")
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+
+def test_sod_256_200_steps_matches_oracle_and_exact():
+    c = cases.sod(n_cell=(256, 4, 4), order=5, max_grid=64)
+    g = Mflo(c, device="cuda")
+    o = OracleLevel(c)
+    for _ in range(200):
+        dt = o.compute_dt()
+        o.advance(dt)
+        g.advance(dt, norms=False)
+    sg, so = g.state(), o.state()
+    for comp in range(abi.FLO_NVARS):
+        ref = so[comp]
+        scale = max(np.linalg.norm(ref), 1e-300)
+        assert np.linalg.norm(sg[comp] - ref) / scale <= 1e-10, comp
+    x = (np.arange(256) + 0.5) / 256 - 0.5
+    ex = riemann.sample(x, o.time, 1, 0, 1, 0.125, 0, 0.1)
+    assert np.abs(sg[abi.RHO][0, 0, :] - ex[0]).mean() < 0.004
+
+
+def totals(state, ns):
+    comps = [abi.RHO, abi.RHOU, abi.RHOV, abi.RHOW, abi.RHOE] + [abi.FLO_NVARS + s for s in range(ns)]
+    return np.array([state[c].sum(dtype=np.float64) for c in comps]), np.array(
+        [np.abs(state[c]).sum(dtype=np.float64) for c in comps])
+
+
+def test_taylor_green_256_conserves():
+    c = cases.taylor_green_mix(n=256, order=5, max_grid=64)
+    g = Mflo(c, device="cuda", only_flow=True)
+    t0, a0 = totals(c.state, c.params.nspec)
+    dt = g.compute_dt()
+    for _ in range(2):
+        g.advance(dt, norms=False)
+    t1, _ = totals(g.state(), c.params.nspec)
+    # relative to the summed magnitudes: the momenta of the vortex sum to ~0
+    assert np.all(np.abs(t1 - t0) <= 1e-12 * a0), (t1 - t0) / a0
+
+
+def test_ib_256_cache_and_batched_forms_are_bitwise_equal():
+    """The per-box step with and without the cut-cell cache and the batched
+    step over all boxes give bitwise equal states at full size.  (Box-layout
+    invariance does not hold with immersed boundaries, here or in the
+    reference: update_cutcell_data updates each box's valid cut cells only, so
+    a cut cell seen as a ghost of a neighbouring box keeps its filled value,
+    Source/mflo_evolve.cpp:509-518.)"""
+    c = cases.porous_ib(n=256, order=2, max_grid=64)
+    lib = abi.load()
+    abi.check("mfg_init", lib.mfg_init(C.byref(c.params)))
+    s = torch.cuda.Stream()
+    st = C.c_void_p(s.cuda_stream)
+    dt = 5e-10
+    out = []
+    for form in ("cached", "uncached", "batched"):
+        abi.check("mfg_set_cutcell_cache", lib.mfg_set_cutcell_cache(int(form != "uncached")))
+        lev = Level(c.boxes, c.ncomp, backend="torch", device="cuda", with_dsdt=False)
+        lev.set_state(c.state)
+        desc = lev.descriptors()
+        with torch.cuda.stream(s):
+            if form == "batched":
+                geoms = (abi.Geom * 1)(c.geom)
+                h = C.c_void_p()
+                abi.check("mfg_boxlist_create", lib.mfg_boxlist_create(desc, len(c.boxes), geoms, 1, C.byref(h)))
+                for _ in range(2):
+                    abi.check("mfg_boxlist_step", lib.mfg_boxlist_step(h, 0.0, dt, 1, st))
+                s.synchronize()
+                lib.mfg_boxlist_destroy(h)
+            else:
+                for _ in range(2):
+                    abi.check("mfg_advance_level", lib.mfg_advance_level(desc, len(c.boxes), C.byref(c.geom), 0.0, dt,
+                                                                         0, 1, None, st))
+                s.synchronize()
+        out.append(lev.get_state(c.shape_zyx))
+        del lev
+        torch.cuda.empty_cache()
+    abi.check("mfg_set_cutcell_cache", lib.mfg_set_cutcell_cache(1))
+    assert np.array_equal(out[0], out[1])
+    assert np.array_equal(out[0], out[2])
