@@ -1,7 +1,10 @@
 """Batched AMR form (mfg_boxlist_*): the batched launches and the CUDA-graph
-replay give bit-identical states to the plain per-box launches of the same
-kernels, on one level (where the per-box path is itself parity-tested against
-the oracle) and on a multi-level hierarchy of uneven boxes."""
+replay give the states of the plain per-box launches of the same kernel
+bodies, on one level (where the per-box path is itself parity-tested against
+the oracle) and on a multi-level hierarchy of uneven boxes: bitwise on the
+catalyst configurations, to the parity tolerance on the porous one (the
+batched and per-box kernels are compiled separately and the compiler may
+contract a multiply and an add differently in each)."""
 import ctypes as C
 
 import numpy as np
@@ -42,6 +45,36 @@ def test_batched_single_level_equals_per_box_step():
     s.synchronize()
     lib.mfg_boxlist_destroy(h)
     assert np.array_equal(a.get_state(c.shape_zyx), b.get_state(c.shape_zyx))
+
+
+@pytest.mark.parametrize("order", [2, 5])
+def test_batched_porous_matches_per_box_step(order):
+    """Pressure inlet/outlet, single-gas thermo: the batched step equals the
+    per-box step to the parity tolerance (1e-12 of each component's domain
+    maximum; the two are separate kernels, whose multiply-add contraction the
+    compiler chooses independently, so equality is to the last bits)."""
+    from helpers import rel_err
+    c = perturb(cases.porous_ib(n=32, order=order, max_grid=16), 31, vel_amp=1e-2)
+    lib = abi.load()
+    abi.check("mfg_init", lib.mfg_init(C.byref(c.params)))
+    a = Level(c.boxes, c.ncomp, backend="torch", device="cuda")
+    b = Level(c.boxes, c.ncomp, backend="torch", device="cuda")
+    a.set_state(c.state)
+    b.set_state(c.state)
+    s = torch.cuda.Stream()
+    st = C.c_void_p(s.cuda_stream)
+    geoms = (abi.Geom * 1)(c.geom)
+    h = _boxlist(lib, b.descriptors(), len(c.boxes), geoms, 1)
+    dt = 5e-10
+    with torch.cuda.stream(s):
+        for _ in range(2):
+            abi.check("mfg_advance_level", lib.mfg_advance_level(a.descriptors(), len(c.boxes), C.byref(c.geom),
+                                                                 0.0, dt, 0, 1, None, st))
+            abi.check("mfg_boxlist_step", lib.mfg_boxlist_step(h, 0.0, dt, 1, st))
+    s.synchronize()
+    lib.mfg_boxlist_destroy(h)
+    err, comp = rel_err(b.get_state(c.shape_zyx), a.get_state(c.shape_zyx))
+    assert err <= 1e-12, (err, comp)
 
 
 @pytest.mark.parametrize("order", [5, 2])

@@ -10,7 +10,10 @@ properties that do not need the oracle to finish a 256^3 run:
   and species mass are conserved to 1e-12 of the summed magnitudes over two
   steps (the face fluxes telescope on a periodic box).
 * 256^3 immersed boundary, order 2: the per-box step with and without the
-  cut-cell cache and the batched step give bitwise equal states.
+  cut-cell cache give bitwise equal states, and the batched step equals them
+  to the parity tolerance (1e-12 of each component's domain maximum): the
+  batched tile kernels and the per-box kernels are separate kernels, for
+  which the compiler may contract a multiply and an add differently.
 """
 import ctypes as C
 
@@ -20,6 +23,7 @@ import pytest
 from mesoflow_gb300 import abi, cases
 from mesoflow_gb300.driver import Mflo
 from mesoflow_gb300.level import Level
+from helpers import rel_err
 from oracle_run import OracleLevel
 import riemann
 
@@ -63,9 +67,10 @@ def test_taylor_green_256_conserves():
     assert np.all(np.abs(t1 - t0) <= 1e-12 * a0), (t1 - t0) / a0
 
 
-def test_ib_256_cache_and_batched_forms_are_bitwise_equal():
-    """The per-box step with and without the cut-cell cache and the batched
-    step over all boxes give bitwise equal states at full size.  (Box-layout
+def test_ib_256_cache_and_batched_forms_agree():
+    """The per-box step with and without the cut-cell cache give bitwise equal
+    states at full size, and the batched step over all boxes equals them to
+    the parity tolerance.  (Box-layout
     invariance does not hold with immersed boundaries, here or in the
     reference: update_cutcell_data updates each box's valid cut cells only, so
     a cut cell seen as a ghost of a neighbouring box keeps its filled value,
@@ -101,4 +106,5 @@ def test_ib_256_cache_and_batched_forms_are_bitwise_equal():
         torch.cuda.empty_cache()
     abi.check("mfg_set_cutcell_cache", lib.mfg_set_cutcell_cache(1))
     assert np.array_equal(out[0], out[1])
-    assert np.array_equal(out[0], out[2])
+    err, comp = rel_err(out[2], out[0])
+    assert err <= 1e-12, (err, comp)
