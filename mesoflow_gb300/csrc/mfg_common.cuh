@@ -109,6 +109,32 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 __device__ __forceinline__ bool below_one(double v) { return __double_as_longlong(v) < 0x3FF0000000000000LL; }
 __device__ __forceinline__ bool is_one(double v) { return __double_as_longlong(v) == 0x3FF0000000000000LL; }
 
+// Comparisons and min/max on the integer pipe.  For doubles >= 0 the IEEE
+// order is the order of the bit patterns read as signed 64-bit integers, so
+// these select exactly what the FP64 forms select (NaN aside).
+__device__ __forceinline__ bool abs_le(double x, double c) {  // |x| <= c, c > 0
+    return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) <= __double_as_longlong(c);
+}
+__device__ __forceinline__ bool nonneg_le(double x, double c) {  // x <= c for x >= 0
+    return __double_as_longlong(x) <= __double_as_longlong(c);
+}
+__device__ __forceinline__ bool nonneg_ge(double x, double c) {  // x >= c for x >= 0
+    return __double_as_longlong(x) >= __double_as_longlong(c);
+}
+__device__ __forceinline__ bool is_positive(double x) { return __double_as_longlong(x) > 0; }  // x > 0
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    return __longlong_as_double(ia > ib ? ia : ib);
+}
+__device__ __forceinline__ double min_nonneg(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    return __longlong_as_double(ia < ib ? ia : ib);
+}
+__device__ __forceinline__ double pos_part(double x) { return is_positive(x) ? x : 0.0; }  // max(x, 0)
+__device__ __forceinline__ bool is_nan(double x) {
+    return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+}
+
 // Reciprocal of a positive, finite, normal x: the hardware approximation
 // (PTX rcp.approx.ftz.f64) refined by two Newton-Raphson steps
 // r <- r + r (1 - x r), each of which squares the relative error, so the

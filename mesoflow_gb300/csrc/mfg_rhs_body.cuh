@@ -86,22 +86,28 @@ __device__ __forceinline__ void weno_face(const double s[6], double& up, double&
     um = weno_edge<true, FAST>(s[5], s[4], s[3], s[2], s[1]);
 }
 
-// AUSM+-up split functions (flux_schemes.H:107-181), beta = 1/8.
+// AUSM+-up split functions (flux_schemes.H:107-181), beta = 1/8.  The
+// supersonic branches of the pressure splits, (M + |M|)/(2M) and
+// (M - |M|)/(2M), are exactly 1 or 0 (with a zero's sign that no later
+// operation keeps), so they are selected instead of divided; the |M| <= 1
+// tests run on the integer pipe.
 __device__ __forceinline__ double split_mach_p(double M) {
-    return (fabs(M) <= 1.0) ? (0.25 * (M + 1.0)) * (M + 1.0) + (0.125 * (M * M - 1.0)) * (M * M - 1.0)
-                            : 0.5 * (M + fabs(M));
+    return abs_le(M, 1.0) ? (0.25 * (M + 1.0)) * (M + 1.0) + (0.125 * (M * M - 1.0)) * (M * M - 1.0)
+                          : 0.5 * (M + fabs(M));
 }
 __device__ __forceinline__ double split_mach_m(double M) {
-    return (fabs(M) <= 1.0) ? (-0.25 * (M - 1.0)) * (M - 1.0) - (0.125 * (M * M - 1.0)) * (M * M - 1.0)
-                            : 0.5 * (M - fabs(M));
+    return abs_le(M, 1.0) ? (-0.25 * (M - 1.0)) * (M - 1.0) - (0.125 * (M * M - 1.0)) * (M * M - 1.0)
+                          : 0.5 * (M - fabs(M));
 }
 __device__ __forceinline__ double split_pres_p(double M, double alpha) {
-    return (fabs(M) <= 1.0) ? ((0.25 * (M + 1.0)) * (M + 1.0)) * (2.0 - M) + ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
-                            : (0.5 * (M + fabs(M))) / M;
+    return abs_le(M, 1.0)
+               ? ((0.25 * (M + 1.0)) * (M + 1.0)) * (2.0 - M) + ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
+               : (is_positive(M) ? 1.0 : 0.0);
 }
 __device__ __forceinline__ double split_pres_m(double M, double alpha) {
-    return (fabs(M) <= 1.0) ? ((0.25 * (M - 1.0)) * (M - 1.0)) * (2.0 + M) - ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
-                            : (0.5 * (M - fabs(M))) / M;
+    return abs_le(M, 1.0)
+               ? ((0.25 * (M - 1.0)) * (M - 1.0)) * (2.0 + M) - ((alpha * M) * (M * M - 1.0)) * (M * M - 1.0)
+               : (is_positive(M) ? 0.0 : 1.0);
 }
 
 // MUSCL state of component c with the Tatsumi-Martinelli-Jameson limiter
@@ -137,15 +143,17 @@ __device__ __forceinline__ void prim_body(const RhsBox& B, int64_t t) {
     double spec[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) spec[s] = (s < c_P.nspec) ? S.p[o + (NFLO + s) * S.ns] : 0.0;
-    // cons_to_prim (consprim_funcs.H:9-23)
-    const double vx = m0 / rho, vy = m1 / rho, vz = m2 / rho;
+    // cons_to_prim (consprim_funcs.H:9-23); one Newton-refined reciprocal of
+    // the density replaces the reference's five divisions by it
+    const double irho = rcp_pos(rho);
+    const double vx = m0 * irho, vy = m1 * irho, vz = m2 * irho;
     const double rhoe = E - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
     const double pf = thermo_p<NS>(rhoe, rho, spec);
     // get_max_eigenvalue's own-species terms (flux_schemes.H:21-43)
-    const double reig = E - (0.5 * ((m0 * m0 + m1 * m1) + m2 * m2)) / rho;
+    const double reig = E - (0.5 * ((m0 * m0 + m1 * m1) + m2 * m2)) * irho;
     const double peig = thermo_p<NS>(reig, rho, spec);
     const double gam = thermo_gamma<NS>(rho, spec);
-    const double aown = sqrt((gam * peig) / rho);
+    const double aown = sqrt((gam * peig) * irho);
     const Fab& X = B.aux;
     const int64_t q = X.off(c.i, c.j, c.k);
     X.p[q + AUX_VX * X.ns] = vx;
@@ -181,7 +189,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
 #pragma unroll
     for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
     const double facevfrac = 0.5 * (vf[oL] + vf[oR]);
-    const bool active = P.do_ns && (facevfrac >= 0.5);
+    const bool active = P.do_ns && nonneg_ge(facevfrac, 0.5);
 
     double fs[NFS];
 #pragma unroll
@@ -196,7 +204,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             const int64_t qL = X.off(f.i, f.j, f.k) - ((d == 0) ? 1 : (d == 1) ? X.js : X.ks);
             const int64_t qR = X.off(f.i, f.j, f.k);
             const double* vd = X.p + (AUX_VX + d) * X.ns;
-            const double veln = fmax(fabs(vd[qL]), fabs(vd[qR]));
+            const double veln = max_nonneg(fabs(vd[qL]), fabs(vd[qR]));
             const double aL = X.p[qL + AUX_AOWN * X.ns];
             double aR;
             if (ord == 5) {
@@ -210,7 +218,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             } else {
                 aR = X.p[qR + AUX_AOWN * X.ns];
             }
-            fs[FS_LAMBDA] = fmax(aL, aR) + veln;
+            fs[FS_LAMBDA] = max_nonneg(aL, aR) + veln;
         } else {
             // AUSM+-up (flux_schemes.H:185-310) on first- or second-order states
             const int nc = NCONS + P.nspec;
@@ -240,23 +248,32 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             const double vL = (d == 0) ? vxL : (d == 1) ? vyL : vzL;
             const double vR = (d == 0) ? vxR : (d == 1) ? vyR : vzR;
             const bool cg = P.thermo_kind == MFG_THERMO_MASS_SINGLE;
-            const double HL = (cg ? P.g_gm1 : gL / (gL - 1.0)) * (pL * irL) + 0.5 * kL;
-            const double HR = (cg ? P.g_gm1 : gR / (gR - 1.0)) * (pR * irR) + 0.5 * kR;
+            // gamma/(gamma-1) and 2(gamma-1)/(gamma+1): constants of the single-gas
+            // family, else per face state with reciprocals of the positive gamma +- 1
+            double gfL = P.g_gm1, gfR = P.g_gm1, afL = P.astar_fac, afR = P.astar_fac;
+            if (!cg) {
+                gfL = gL * rcp_pos(gL - 1.0);
+                gfR = gR * rcp_pos(gR - 1.0);
+                afL = (2.0 * (gL - 1.0)) * rcp_pos(gL + 1.0);
+                afR = (2.0 * (gR - 1.0)) * rcp_pos(gR + 1.0);
+            }
+            const double HL = gfL * (pL * irL) + 0.5 * kL;
+            const double HR = gfR * (pR * irR) + 0.5 * kR;
             const double rho_half = 0.5 * (rL + rR);
-            double as2 = (cg ? P.astar_fac : (2.0 * (gL - 1.0)) / (gL + 1.0)) * HL;
-            const double ahL = as2 * rcp_pos(fmax(sqrt(as2), fabs(vL)));
-            as2 = (cg ? P.astar_fac : (2.0 * (gR - 1.0)) / (gR + 1.0)) * HR;
-            const double ahR = as2 * rcp_pos(fmax(sqrt(as2), fabs(vR)));
-            const double ah = fmin(ahL, ahR);
+            double as2 = afL * HL;
+            const double ahL = as2 * rcp_pos(max_nonneg(sqrt(as2), fabs(vL)));
+            as2 = afR * HR;
+            const double ahR = as2 * rcp_pos(max_nonneg(sqrt(as2), fabs(vR)));
+            const double ah = min_nonneg(ahL, ahR);
             const double iah = rcp_pos(ah);
             const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
             const double Mb2 = (0.5 * (vL * vL + vR * vR)) * (iah * iah);
-            const double Mo = sqrt(fmin(1.0, fmax(Mb2, 0.3 * 0.3)));
+            const double Mo = sqrt(min_nonneg(1.0, max_nonneg(Mb2, 0.3 * 0.3)));
             const double fa = Mo * (2.0 - Mo);
-            Mh = Mh - ((fmax(1.0 - Mb2, 0.0) * (pR - pL)) * (iah * iah)) * (0.25 * rcp_pos(fa * rho_half));
+            Mh = Mh - ((pos_part(1.0 - Mb2) * (pR - pL)) * (iah * iah)) * (0.25 * rcp_pos(fa * rho_half));
             double modM = fabs(Mh);
-            if (modM <= 0.3) modM = (Mh * Mh + 0.3 * 0.3) / (2.0 * 0.3);
+            if (nonneg_le(modM, 0.3)) modM = (Mh * Mh + 0.3 * 0.3) * (1.0 / (2.0 * 0.3));
             const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
             const double PLp = split_pres_p(ML, alpha), PRm = split_pres_m(MR, alpha);
             double ph = PLp * pL + PRm * pR;
@@ -513,14 +530,15 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
     }
     const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
     const int nnull = (P.species_in_solid == 1) ? NFLO : NFLO + P.nspec;
+    // vfrac tests and the NaN test on the integer pipe
     if (n != RHOE) {
-        if (n < nnull && vfrac < 1.0) ds = 0.0;
+        if (n < nnull && below_one(vfrac)) ds = 0.0;
     } else if (!P.conj_ht) {
-        if (vfrac < 1.0) ds = 0.0;
-    } else if (vfrac > 0.0 && vfrac < 1.0) {
+        if (below_one(vfrac)) ds = 0.0;
+    } else if (is_positive(vfrac) && below_one(vfrac)) {
         ds = 0.0;
     }
-    if (ds != ds) raise_status(MFG_STATUS_NAN);
+    if (is_nan(ds)) raise_status(MFG_STATUS_NAN);
     if (B.dsdt.p) B.dsdt(x.i, x.j, x.k, n) = ds;
     if (stage == 1) {
         B.snew(x.i, x.j, x.k, n) = add(B.sb(x.i, x.j, x.k, n), mul(dt, ds));
