@@ -290,42 +290,36 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double* V1 = S.p + VELY * S.ns;
         const double* V2 = S.p + VELZ * S.ns;
         const double ids = B.idx[d], ih1 = 0.5 * B.idx[t1], ih2 = 0.5 * B.idx[t2];
-        double g[3][3];  // g[component][0: normal, 1: trans1, 2: trans2]
-        const double* Vc[3] = {V0, V1, V2};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const double* V = Vc[a];
-            g[a][0] = (V[oR] - V[oL]) * ids;
-            g[a][1] = (0.5 * (V[oL + st1] + V[oR + st1]) - 0.5 * (V[oL - st1] + V[oR - st1])) * ih1;
-            g[a][2] = (0.5 * (V[oL + st2] + V[oR + st2]) - 0.5 * (V[oL - st2] + V[oR - st2])) * ih2;
-        }
-        // gradient along Cartesian axis x/y/z is the entry whose sweep role maps to it
-        const int gx = (d == 0) ? 0 : (d == 1) ? 2 : 1;
-        const int gy = (d == 0) ? 1 : (d == 1) ? 0 : 2;
-        const int gz = (d == 0) ? 2 : (d == 1) ? 1 : 0;
-        const double dudx = g[0][gx], dudy = g[0][gy], dudz = g[0][gz];
-        const double dvdx = g[1][gx], dvdy = g[1][gy], dvdz = g[1][gz];
-        const double dwdx = g[2][gx], dwdy = g[2][gy], dwdz = g[2][gz];
+        // Only the stress row of the face normal is needed: tau_{d a} uses the
+        // normal derivatives of all three velocities, the two transverse
+        // derivatives of the normal velocity, and the divergence's two other
+        // diagonal terms (7 of the 9 gradients, 3 of the 9 stresses).
+        const double* Vd = (d == 0) ? V0 : (d == 1) ? V1 : V2;
+        const double* Vt1 = (t1 == 0) ? V0 : (t1 == 1) ? V1 : V2;
+        const double* Vt2 = (t2 == 0) ? V0 : (t2 == 1) ? V1 : V2;
+        const double gn0 = (V0[oR] - V0[oL]) * ids, gn1 = (V1[oR] - V1[oL]) * ids, gn2 = (V2[oR] - V2[oL]) * ids;
+        const double d_t1 = (0.5 * (Vd[oL + st1] + Vd[oR + st1]) - 0.5 * (Vd[oL - st1] + Vd[oR - st1])) * ih1;
+        const double d_t2 = (0.5 * (Vd[oL + st2] + Vd[oR + st2]) - 0.5 * (Vd[oL - st2] + Vd[oR - st2])) * ih2;
+        const double t1_t1 = (0.5 * (Vt1[oL + st1] + Vt1[oR + st1]) - 0.5 * (Vt1[oL - st1] + Vt1[oR - st1])) * ih1;
+        const double t2_t2 = (0.5 * (Vt2[oL + st2] + Vt2[oR + st2]) - 0.5 * (Vt2[oL - st2] + Vt2[oR - st2])) * ih2;
+        // du/dx, dv/dy, dw/dz: the normal derivative along d, else the transverse one
+        const double dudx = (d == 0) ? gn0 : (t1 == 0) ? t1_t1 : t2_t2;
+        const double dvdy = (d == 1) ? gn1 : (t1 == 1) ? t1_t1 : t2_t2;
+        const double dwdz = (d == 2) ? gn2 : (t1 == 2) ? t1_t1 : t2_t2;
         // viscosity always from cells (i,j,k) and (i-1,j,k) (compute_flux_3d.H:179)
         const double mu = (P.visc_mode == MFG_TRANSPORT_CONST)
                               ? P.visc_hm
                               : harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR]),
                                               blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR - 1]));
         const double delu = (dudx + dvdy) + dwdz;
-        double tau[3][3];
-        tau[0][0] = mu * (2.0 * dudx - kTwo3rd * delu);
-        tau[0][1] = mu * (dudy + dvdx);
-        tau[0][2] = mu * (dudz + dwdx);
-        tau[1][0] = mu * (dvdx + dudy);
-        tau[1][1] = mu * (2.0 * dvdy - kTwo3rd * delu);
-        tau[1][2] = mu * (dvdz + dwdy);
-        tau[2][0] = mu * (dwdx + dudz);
-        tau[2][1] = mu * (dwdy + dvdz);
-        tau[2][2] = mu * (2.0 * dwdz - kTwo3rd * delu);
+        const double gn[3] = {gn0, gn1, gn2};
         const double fvel[3] = {0.5 * (V0[oL] + V0[oR]), 0.5 * (V1[oL] + V1[oR]), 0.5 * (V2[oL] + V2[oR])};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const double tn = tau[d][a];  // tau_{ja} n_j with n = e_d
+            // tau_{d a}: mu (2 dV_d/dx_d - 2/3 div V) on the diagonal, else
+            // mu (dV_d/dx_a + dV_a/dx_d)
+            const double tn = (a == d) ? mu * (2.0 * gn[a] - kTwo3rd * delu)
+                                       : mu * (gn[a] + ((a == t1) ? d_t1 : d_t2));
             fs[FS_VIS + a] = tn;
             fs[FS_VISE + a] = tn * fvel[a];
         }
