@@ -66,11 +66,13 @@ __device__ void dpres(double rhoe, const double* c, double& dp_drhoe, double* dp
             cvs += P.cv[s] * c[s];
             S += c[s];
         }
-    const double T = rhoe / cvs;
-    dp_drhoe = P.R_univ * S / cvs;
+    const double icvs = 1.0 / cvs;
+    const double T = rhoe * icvs;
+    dp_drhoe = P.R_univ * S * icvs;
+    const double RT = P.R_univ * T, Sic = S * icvs;
 #pragma unroll
     for (int s = 0; s < NS; ++s)
-        if (s < P.ngas) dp_dc[s] = P.R_univ * T * (1.0 - S * P.cv[s] / cvs);
+        if (s < P.ngas) dp_dc[s] = RT * (1.0 - Sic * P.cv[s]);
 }
 
 // dgamma/dc_k of gamma = 1 + 1/A, A = sum_s (c_s/S)/(gamma_s - 1)
@@ -80,16 +82,21 @@ __device__ void dgamma(const double* c, double* dg_dc) {
 #pragma unroll
     for (int s = 0; s < NS; ++s) dg_dc[s] = 0.0;
     if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return;
-    double S = 0.0, A = 0.0;
+    // 1/(gamma_s - 1) = cv_s / R for the molar families
+    double S = 0.0, Ac = 0.0;
+    const double iR = 1.0 / P.R_univ;
 #pragma unroll
     for (int s = 0; s < NS; ++s)
-        if (s < P.ngas) S += c[s];
+        if (s < P.ngas) {
+            S += c[s];
+            Ac += c[s] * P.cv[s];
+        }
+    const double iS = 1.0 / S;
+    const double A = Ac * iR * iS;
+    const double k = -iS / (A * A);
 #pragma unroll
     for (int s = 0; s < NS; ++s)
-        if (s < P.ngas) A += (c[s] / S) / (P.gamma[s] - 1.0);
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-        if (s < P.ngas) dg_dc[s] = -(1.0 / (A * A)) * ((1.0 / (P.gamma[s] - 1.0)) - A) / S;
+        if (s < P.ngas) dg_dc[s] = k * (P.cv[s] * iR - A);
 }
 
 // T(rho, p, c) partials
@@ -504,14 +511,15 @@ __global__ void __launch_bounds__(AT) adj_aux_kernel(AdjBox A) {
     double spec[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? S.p[o + (NFLO + s) * S.ns] : 0.0;
-    const double v[3] = {m[0] / rho, m[1] / rho, m[2] / rho};
+    const double irho = 1.0 / rho;
+    const double v[3] = {m[0] * irho, m[1] * irho, m[2] * irho};
     const double k2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
     const double rhoe = E - (0.5 * rho) * k2;
     const double mm = (m[0] * m[0] + m[1] * m[1]) + m[2] * m[2];
-    const double reig = E - (0.5 * mm) / rho;
+    const double reig = E - (0.5 * mm) * irho;
     const double peig = thermo_p<NS>(reig, rho, spec);
     const double gam = thermo_gamma<NS>(rho, spec);
-    const double qa = (gam * peig) / rho;
+    const double qa = (gam * peig) * irho;
     const double aown = sqrt(qa);
     double rb = 0.0, mb[3] = {0, 0, 0}, Eb = 0.0, sb[NS];
 #pragma unroll
@@ -519,10 +527,10 @@ __global__ void __launch_bounds__(AT) adj_aux_kernel(AdjBox A) {
     double vb[3] = {ab[AUX_VX], ab[AUX_VY], ab[AUX_VZ]};
     double gb = ab[AUX_GAM], reb = ab[AUX_REIG];
     if (ab[AUX_AOWN] != 0.0) {  // a = sqrt(gamma p_eig / rho)
-        const double qb = ab[AUX_AOWN] / (2.0 * aown);
-        gb += qb * peig / rho;
-        const double pb = qb * gam / rho;
-        rb -= qb * qa / rho;
+        const double qb = ab[AUX_AOWN] * (0.5 / aown);
+        gb += qb * peig * irho;
+        const double pb = qb * gam * irho;
+        rb -= qb * qa * irho;
         double dpr, dpc[NS];
         dpres<NS>(reig, spec, dpr, dpc);
         reb += pb * dpr;
@@ -537,8 +545,8 @@ __global__ void __launch_bounds__(AT) adj_aux_kernel(AdjBox A) {
     }
     // rho e_eig = E - (m.m)/(2 rho)
     Eb += reb;
-    for (int a = 0; a < 3; ++a) mb[a] -= reb * m[a] / rho;
-    rb += reb * (0.5 * mm) / (rho * rho);
+    for (int a = 0; a < 3; ++a) mb[a] -= reb * v[a];
+    rb += reb * (0.5 * mm) * (irho * irho);
     // p = p(E - rho |v|^2 / 2, c)
     if (ab[AUX_PF] != 0.0) {
         double dpr, dpc[NS];
@@ -552,8 +560,8 @@ __global__ void __launch_bounds__(AT) adj_aux_kernel(AdjBox A) {
     }
     // v = m / rho
     for (int a = 0; a < 3; ++a) {
-        mb[a] += vb[a] / rho;
-        rb -= vb[a] * m[a] / (rho * rho);
+        mb[a] += vb[a] * irho;
+        rb -= vb[a] * v[a] * irho;
     }
     aadd(&G.p[o + RHO * G.ns], rb);
     for (int a = 0; a < 3; ++a) aadd(&G.p[o + (RHOU + a) * G.ns], mb[a]);
@@ -907,18 +915,17 @@ __device__ double rate_k(int r, double kr, const double* c, double* dc) {
     double cm = 1.0;
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
-        const double o = P.order[r][s];
-        if (s < P.nspec && o > 0.0) cm *= cpow(c[s], o);
+        if ((P.ord_mask[r] >> s) & 1u) cm *= cpow(c[s], P.order[r][s]);
     }
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
         dc[j] = 0.0;
-        if (j >= P.nspec || !(P.order[r][j] > 0.0)) continue;
+        if (!((P.ord_mask[r] >> j) & 1u)) continue;
         double pr = kr;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
+            if (!((P.ord_mask[r] >> s) & 1u)) continue;
             const double o = P.order[r][s];
-            if (s >= P.nspec || !(o > 0.0)) continue;
             pr *= (s == j) ? dcpow(c[s], o) : cpow(c[s], o);
         }
         dc[j] = pr;
@@ -936,13 +943,12 @@ __device__ void wdot_k(const double* c, const double* kr, double* w) {
         double cm = 1.0;
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
-            const double o = P.order[r][s];
-            if (s < P.nspec && o > 0.0) cm *= cpow(c[s], o);
+            if ((P.ord_mask[r] >> s) & 1u) cm *= cpow(c[s], P.order[r][s]);
         }
         const double rate = kr[r] * cm;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
-            if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) w[s] += P.nu[r][s] * rate;
+            if ((P.nu_mask[r] >> s) & 1u) w[s] += P.nu[r][s] * rate;
     }
 }
 
@@ -956,7 +962,7 @@ __device__ void wdot_vjp(const double* c, const double* kr, const double* eT, co
         double rb = 0.0;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
-            if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) rb += P.nu[r][s] * fb[s];
+            if ((P.nu_mask[r] >> s) & 1u) rb += P.nu[r][s] * fb[s];
         if (rb == 0.0) continue;
         double dc[NS];
         const double rate = rate_k<NS>(r, kr[r], c, dc);

@@ -235,6 +235,8 @@ int mfg_init(const mfg_params* p) {
         for (int s = 0; s < MFG_MAX_SPECIES; ++s) {
             h.nu[r][s] = p->nu[r][s];
             h.order[r][s] = p->order[r][s];
+            if (s < p->nspec && p->order[r][s] > 0.0) h.ord_mask[r] |= 1u << s;
+            if (s < p->nspec && std::fabs(p->nu[r][s]) > 0.0) h.nu_mask[r] |= 1u << s;
         }
     }
     for (int d = 0; d < 3; ++d) {

@@ -76,11 +76,10 @@ struct PhaseTiles {
 
 __device__ __forceinline__ void grown_of(const MBox& b, long long t, int& i, int& j, int& k) {
     const int l0 = b.hi[0] - b.lo[0] + 1 + 2 * MFG_NGROW, l1 = b.hi[1] - b.lo[1] + 1 + 2 * MFG_NGROW;
-    const long long a = t / l0;
-    i = b.lo[0] - MFG_NGROW + (int)(t - a * l0);
-    const long long kk = a / l1;
-    k = b.lo[2] - MFG_NGROW + (int)kk;
-    j = b.lo[1] - MFG_NGROW + (int)(a - kk * l1);
+    split3(t, l0, l1, i, j, k);
+    i += b.lo[0] - MFG_NGROW;
+    j += b.lo[1] - MFG_NGROW;
+    k += b.lo[2] - MFG_NGROW;
 }
 
 __device__ __forceinline__ int owner_at(const LevelG& G, const int* owner, const int w[3]) {

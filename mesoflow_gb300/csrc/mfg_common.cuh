@@ -48,6 +48,9 @@ struct DevParams {
     double nu[MAXR][MAXS];
     double order[MAXR][MAXS];
     double A[MAXR], Ea[MAXR];
+    // sparsity of the reaction table as bit masks over the species (bit s:
+    // order[r][s] > 0, resp. nu[r][s] != 0), so the kernels test integers
+    unsigned ord_mask[MAXR], nu_mask[MAXR];
     int bc_lo[3], bc_hi[3];
     mfg_extbc ext_lo[3], ext_hi[3];
 };
@@ -108,6 +111,19 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 // FP64 compare (the FP64 pipe is the bottleneck of these kernels).
 __device__ __forceinline__ bool below_one(double v) { return __double_as_longlong(v) < 0x3FF0000000000000LL; }
 __device__ __forceinline__ bool is_one(double v) { return __double_as_longlong(v) == 0x3FF0000000000000LL; }
+
+// Offsets (a0, a1, a2) of linear item t of an l0 x l1 x n2 box, a0 fastest.
+// Every per-box item count fits in 32 bits, so 32-bit divisions serve (a
+// 64-bit division is a long instruction sequence, comparable to the FP64
+// work of the small per-(cell, component) kernels).
+__device__ __forceinline__ void split3(int64_t t, int l0, int l1, int& a0, int& a1, int& a2) {
+    const unsigned u = (unsigned)t, n0 = (unsigned)l0, n1 = (unsigned)l1;
+    const unsigned q = u / n0;
+    const unsigned q2 = q / n1;
+    a0 = (int)(u - q * n0);
+    a1 = (int)(q - q2 * n1);
+    a2 = (int)q2;
+}
 
 // Comparisons and min/max on the integer pipe.  For doubles >= 0 the IEEE
 // order is the order of the bit patterns read as signed 64-bit integers, so

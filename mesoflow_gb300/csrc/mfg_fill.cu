@@ -33,11 +33,10 @@ __device__ __forceinline__ void grown_cell(const FillBox& b, int64_t t, int& i, 
     const int l0 = b.hi[0] - b.lo[0] + 1 + 2 * MFG_NGROW, l1 = b.hi[1] - b.lo[1] + 1 + 2 * MFG_NGROW,
               l2 = b.hi[2] - b.lo[2] + 1 + 2 * MFG_NGROW;
     n = (int64_t)l0 * l1 * l2;
-    int64_t a = t / l0;
-    i = b.lo[0] - MFG_NGROW + (int)(t - a * l0);
-    int64_t kk = a / l1;
-    k = b.lo[2] - MFG_NGROW + (int)kk;
-    j = b.lo[1] - MFG_NGROW + (int)(a - kk * l1);
+    split3(t < n ? t : 0, l0, l1, i, j, k);
+    i += b.lo[0] - MFG_NGROW;
+    j += b.lo[1] - MFG_NGROW;
+    k += b.lo[2] - MFG_NGROW;
 }
 
 __global__ void copy_kernel(const FillBox* __restrict__ boxes, FillGeom G, const int* __restrict__ owner, int ncomp) {

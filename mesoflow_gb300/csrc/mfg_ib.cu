@@ -96,9 +96,9 @@ __global__ void cut_vf_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int l1, 
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool diff = false;
     if (t < (int64_t)l0 * l1 * l2) {
-        const int64_t a = t / l0;
-        const int i = lo0 + (int)(t - a * l0), j = lo1 + (int)(a % l1), k = lo2 + (int)(a / l1);
-        const double v = S(i, j, k, VFRAC);
+        int i, j, k;
+        split3(t, l0, l1, i, j, k);
+        const double v = S(lo0 + i, lo1 + j, lo2 + k, VFRAC);
         if (mode == 0)
             vf[t] = v;
         else
@@ -156,8 +156,9 @@ __global__ void cut_commit_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int 
     if (!*dirty || *count > cap) return;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < (int64_t)l0 * l1 * l2) {
-        const int64_t a = t / l0;
-        vf[t] = S(lo0 + (int)(t - a * l0), lo1 + (int)(a % l1), lo2 + (int)(a / l1), VFRAC);
+        int i, j, k;
+        split3(t, l0, l1, i, j, k);
+        vf[t] = S(lo0 + i, lo1 + j, lo2 + k, VFRAC);
     }
     __syncthreads();
     if (threadIdx.x == 0) {

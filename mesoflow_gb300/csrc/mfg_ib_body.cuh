@@ -40,10 +40,10 @@ struct CutCacheView {
 };
 
 __device__ __forceinline__ void cell_of(const CutBox& c, int64_t t, int& i, int& j, int& k) {
-    int64_t a = t / c.len[0];
-    i = c.lo[0] + (int)(t - a * c.len[0]);
-    k = c.lo[2] + (int)(a / c.len[1]);
-    j = c.lo[1] + (int)(a - (int64_t)(k - c.lo[2]) * c.len[1]);
+    split3(t, c.len[0], c.len[1], i, j, k);
+    i += c.lo[0];
+    j += c.lo[1];
+    k += c.lo[2];
 }
 
 // Level-set normal from the central differences of vfrac, the distance to the

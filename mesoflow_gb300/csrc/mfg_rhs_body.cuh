@@ -19,11 +19,11 @@ struct Idx3 {
 };
 
 __device__ __forceinline__ Idx3 delinear(int64_t t, const int lo[3], const int len[3]) {
-    int64_t a = t / len[0];
     Idx3 r;
-    r.i = lo[0] + (int)(t - a * len[0]);
-    r.k = lo[2] + (int)(a / len[1]);
-    r.j = lo[1] + (int)(a - (int64_t)(r.k - lo[2]) * len[1]);
+    split3(t, len[0], len[1], r.i, r.j, r.k);
+    r.i += lo[0];
+    r.j += lo[1];
+    r.k += lo[2];
     return r;
 }
 
@@ -665,11 +665,11 @@ struct WenoWindow {
 // the two cells next to the face, vfL/vfR their volume fractions.
 __device__ __forceinline__ double flux5_face(const RhsBox& B, int d, int c, const Fab& FS, int64_t qf,
                                              const WenoWindow& w, double uL, double uR, double fL, double fR,
-                                             double vfL, double vfR) {
+                                             double vfL, double vfR, bool hyper = true) {
     const DevParams& P = c_P;
     const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
     double F = 0.0;
-    if (flags & 1) {
+    if (hyper && (flags & 1)) {
         const double lam = FS.p[qf + FS_LAMBDA * FS.ns];
         double fp, fm, up, um;
         if (!(flags & 2)) {
@@ -730,6 +730,15 @@ __device__ __forceinline__ void flux5_face_body(const RhsBox& B, int d, int c, i
     const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
     const int64_t xd = (d == 0) ? 1 : (d == 1) ? X.js : X.ks;
     const int64_t oR = S.off(f.i, f.j, f.k), xR = X.off(f.i, f.j, f.k);
+    const double* vfp = S.p + VFRAC * S.ns;
+    const Fab& FS = B.fs[d];
+    if (c >= NCONS && c_P.advect_flag[c - NCONS] == 0.0) {  // not advected: diffusion only
+        const WenoWindow w0 = {};
+        const double F = flux5_face(B, d, c, FS, FS.off(f.i, f.j, f.k), w0, S.p[oR - sd + sc * S.ns],
+                                    S.p[oR + sc * S.ns], 0.0, 0.0, vfp[oR - sd], vfp[oR], false);
+        flux5_store(B, d, c, sc, f, F);
+        return;
+    }
     double ru[6], rf[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) sweep_raw(B, d, c, sc, oR + (q - 3) * sd, xR + (q - 3) * xd, ru[q], rf[q]);
@@ -742,8 +751,6 @@ __device__ __forceinline__ void flux5_face_body(const RhsBox& B, int d, int c, i
     w.f1 = weno_cell(rf[1], rf[2], rf[3]);
     w.f2 = weno_cell(rf[2], rf[3], rf[4]);
     w.f3 = weno_cell(rf[3], rf[4], rf[5]);
-    const double* vfp = S.p + VFRAC * S.ns;
-    const Fab& FS = B.fs[d];
     const double F = flux5_face(B, d, c, FS, FS.off(f.i, f.j, f.k), w, ru[2], ru[3], rf[2], rf[3], vfp[oR - sd],
                                 vfp[oR]);
     flux5_store(B, d, c, sc, f, F);
@@ -777,6 +784,20 @@ __device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, 
     int64_t oR = S.off(iv[0], iv[1], iv[2]);  // right cell of the current face
     int64_t xR = X.off(iv[0], iv[1], iv[2]);
     int64_t qf = FS.off(iv[0], iv[1], iv[2]);
+    const double* vfp = S.p + VFRAC * S.ns;
+    if (c >= NCONS && c_P.advect_flag[c - NCONS] == 0.0) {  // not advected: diffusion only
+        const WenoWindow w0 = {};
+        for (int f = f0; f <= f1; ++f, oR += sd, qf += fd, ++iv[d]) {
+            const double F = flux5_face(B, d, c, FS, qf, w0, S.p[oR - sd + sc * S.ns], S.p[oR + sc * S.ns], 0.0, 0.0,
+                                        vfp[oR - sd], vfp[oR], false);
+            Idx3 fi;
+            fi.i = iv[0];
+            fi.j = iv[1];
+            fi.k = iv[2];
+            flux5_store(B, d, c, sc, fi, F);
+        }
+        return;
+    }
     // raw values of cells f-3 .. f+2
     double ru[6], rf[6];
 #pragma unroll
@@ -792,7 +813,6 @@ __device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, 
     w.f3 = weno_cell(rf[3], rf[4], rf[5]);
     double uL = ru[2], uR = ru[3], uP1 = ru[4], uP2 = ru[5];
     double fL = rf[2], fR = rf[3], fP1 = rf[4], fP2 = rf[5];
-    const double* vfp = S.p + VFRAC * S.ns;
     for (int f = f0;; ++f) {
         const double F = flux5_face(B, d, c, FS, qf, w, uL, uR, fL, fR, vfp[oR - sd], vfp[oR]);
         Idx3 fi;

@@ -168,7 +168,8 @@ cudaError_t launch_clip_species(const mfg_box& b, cudaStream_t st) {
 cudaError_t launch_resnorm_box(const mfg_box& b, double dt, double* partial, double* acc, cudaStream_t st) {
     Valid v = valid_of(b);
     const int nc = NFLO + c_host_params().nspec;
-    int nblk = (int)std::min<int64_t>(1024, (v.n + TPB - 1) / TPB);
+    // 16 cells per thread: blocks of one cell per thread were dominated by their fixed cost
+    int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + 16 * TPB - 1) / (16 * TPB)));
     dim3 g(nblk, nc);
     ProfScope ps(K_RESNORM, st);
     resnorm_kernel<<<g, TPB, 0, st>>>(v, make_fab(b.s_new), make_fab(b.s_old), 1.0 / dt, -1.0 / dt, partial, nblk);

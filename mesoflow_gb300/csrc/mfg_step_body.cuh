@@ -25,10 +25,10 @@ __host__ __device__ inline Valid valid_of(const mfg_box& b) {
 }
 
 __device__ __forceinline__ void cell_of(const Valid& v, int64_t t, int& i, int& j, int& k) {
-    int64_t a = t / v.len[0];
-    i = v.lo[0] + (int)(t - a * v.len[0]);
-    k = v.lo[2] + (int)(a / v.len[1]);
-    j = v.lo[1] + (int)(a - (int64_t)(k - v.lo[2]) * v.len[1]);
+    split3(t, v.len[0], v.len[1], i, j, k);
+    i += v.lo[0];
+    j += v.lo[1];
+    k += v.lo[2];
 }
 
 // Reaction source wdot (chemistry.H compute_spec_source, table form of
@@ -46,7 +46,7 @@ __device__ __forceinline__ void spec_source(const double* spec, double temp, dou
 #pragma unroll
         for (int s = 0; s < NS; ++s) {
             const double o = P.order[r][s];
-            if (s < P.nspec && o > 0.0) {
+            if ((P.ord_mask[r] >> s) & 1u) {
                 const double c = spec[s];
                 cm *= (o == 1.0) ? c : (o == 2.0) ? c * c : pow(c, o);
             }
@@ -56,7 +56,7 @@ __device__ __forceinline__ void spec_source(const double* spec, double temp, dou
         const double rate = kr * cm;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
-            if (s < P.nspec && fabs(P.nu[r][s]) > 0.0) wdot[s] += P.nu[r][s] * rate;
+            if ((P.nu_mask[r] >> s) & 1u) wdot[s] += P.nu[r][s] * rate;
     }
 }
 
