@@ -223,19 +223,6 @@ struct AdjBox {
     Fab lamAux;  // adjoint of the per-cell scalars (grown by 3, NAUX components)
 };
 
-template <int NS>
-__global__ void __launch_bounds__(AT) adj_prim_kernel(RhsBox B) {
-    prim_body<NS>(B, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-// Forward face scalars of direction d (flags, LLF eigenvalue): face_body as
-// in the right-hand side; for order 5 it leaves FS_MH zero, which the
-// per-component pass below uses to accumulate the eigenvalue's adjoint.
-template <int NS>
-__global__ void __launch_bounds__(AT) adj_face_fwd_kernel(RhsBox B, int d) {
-    face_body<NS>(B, d, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
-}
-
 // d(dsdt)/dF: dsdt(cell) = (F(face lo) - F(face hi))/dx, so the adjoint of
 // face f's flux of state component sc is (lamL(right cell) - lamL(left cell))/dx.
 __device__ __forceinline__ double face_bar(const RhsBox& B, const Fab& LL, const Idx3& f, int d, int sc) {
@@ -1125,6 +1112,8 @@ struct Work {
     int nbox = 0, N = 0;
     std::vector<size_t> vcell, gcell;  // per-box offsets in cells
     size_t vtot = 0, gtot = 0;         // cells
+    std::vector<size_t> fsoff;         // per box and direction: offset of its face scalars (doubles)
+    size_t fstot = 0;
     std::vector<double*> owned;
     int* d_owner = nullptr;
     int gran = 1, mlen[3] = {1, 1, 1};
@@ -1219,11 +1208,27 @@ cudaError_t copy_region(const Fab& dst, const Fab& src, const int lo[3], const i
 
 // Forward intermediates of one step.
 struct Snap {
-    double* sb[3];  // stage states after the cut cells (grown)
-    double* s3;     // flow result = chemistry input (valid)
-    double* sc;     // chemistry result (valid)
-    double* sp;     // after the primitive refresh, before clipping (valid)
+    double* sb[3];   // stage states after the cut cells (grown)
+    double* aux[3];  // per-cell primitives of each stage (grown, NAUX components)
+    double* fs[3];   // face scalars of each stage (NFS per face, three directions)
+    double* s3;      // flow result = chemistry input (valid)
+    double* sc;      // chemistry result (valid)
+    double* sp;      // after the primitive refresh, before clipping (valid)
 };
+
+// Points a stage's per-cell primitives and face scalars at box b's part of the
+// snapshot: the forward writes them there, the reverse sweep reads them (for
+// order 5 the face pass leaves FS_MH zero; the reverse sums the eigenvalue's
+// adjoint into it, so each snapshot serves one reverse stage).
+void snap_views(const Work& W, RhsBox& B, const Snap& sn, int stage, int b) {
+    B.aux = W.gfab(sn.aux[stage - 1], b, NAUX);
+    const mfg_box& x = W.boxes[b];
+    for (int d = 0; d < 3; ++d) {
+        const int len[3] = {x.hi[0] - x.lo[0] + 1 + (d == 0), x.hi[1] - x.lo[1] + 1 + (d == 1),
+                            x.hi[2] - x.lo[2] + 1 + (d == 2)};
+        B.fs[d] = dense_fab(sn.fs[stage - 1] + W.fsoff[3 * b + d], x.lo, len);
+    }
+}
 
 // One step on the caller's arrays, as mfg_advance_level (chemistry and
 // clipping on, no norms); with snap the intermediates are saved.
@@ -1247,7 +1252,8 @@ int fwd_step(Work& W, double dt, const Snap* snap, cudaStream_t st) {
                 ADJ_TRY(copy_region(W.gfab(snap->sb[stage - 1], b, N), make_fab(x.sborder), lo, hi, N, st),
                         "forward: stage snapshot");
             }
-            const RhsBox B = layout_rhs_box(x, W.g, W.d_scratch);
+            RhsBox B = layout_rhs_box(x, W.g, W.d_scratch);
+            if (snap) snap_views(W, B, *snap, stage, b);  // keep the stage's primitives and face scalars
             ADJ_TRY(launch_rhs_box(B, stage, dt, weno_fast_mode(), st), "forward: right-hand side");
         }
     }
@@ -1305,23 +1311,17 @@ int adj_step(Work& W, double dt, const Snap& sn, double* lam, double* lamOld, do
             mfg_box x = W.boxes[b];
             x.sborder = W.ga4(sb, b);
             AdjBox A;
+            // forward views of the stage: its state, per-cell primitives and face
+            // scalars as the forward computed them
             A.B = layout_rhs_box(x, W.g, W.d_scratch);
+            snap_views(W, A.B, sn, stage, b);
             A.lamL = W.vfab(lamL, b);
             A.lamSb = W.gfab(lamSb, b, N);
             A.lamAux = W.gfab(lamAux, b, NAUX);
             const int64_t ng = W.grown_cells(b);
-            {
-                ProfScope ps(K_ADJ_CELL, st);
-                ADJ_NS(adj_prim_kernel, (nblk(ng, AT), AT, 0, st), (A.B));
-            }
-            ADJ_TRY(cudaGetLastError(), "reverse: per-cell primitives");
             const int C = NCONS + c_host_params().nspec;
             for (int d = 0; d < 3; ++d) {
                 const unsigned nbf = nblk(face_items(A.B, d), AT);
-                {
-                    ProfScope ps(K_ADJ_FACE_FWD, st);
-                    ADJ_NS(adj_face_fwd_kernel, (nbf, AT, 0, st), (A.B, d));
-                }
                 {
                     ProfScope ps(K_ADJ_FLUX, st);
                     ADJ_NS(adj_flux_kernel, (dim3(nbf, C), AT, 0, st), (A, d));
@@ -1450,6 +1450,10 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
         for (int d = 0; d < 3; ++d) n[d] = boxes[b].hi[d] - boxes[b].lo[d] + 1;
         W.vcell[b] = W.vtot;
         W.gcell[b] = W.gtot;
+        for (int d = 0; d < 3; ++d) {
+            W.fsoff.push_back(W.fstot);
+            W.fstot += face_doubles(n, d, NFS);
+        }
         W.vtot += (size_t)n[0] * n[1] * n[2];
         W.gtot += (size_t)(n[0] + 6) * (n[1] + 6) * (n[2] + 6);
         maxcells = std::max(maxcells, (size_t)n[0] * n[1] * n[2]);
@@ -1525,7 +1529,9 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
     std::vector<Snap> snaps(keep_all ? nsteps : 1);
     for (Snap& sn : snaps) {
         for (int s = 0; s < 3; ++s)
-            if (!(sn.sb[s] = W.grown_buf(W.N))) return MFG_ERR_CUDA;
+            if (!(sn.sb[s] = W.grown_buf(W.N)) || !(sn.aux[s] = W.grown_buf(NAUX)) ||
+                !(sn.fs[s] = W.alloc(W.fstot)))
+                return MFG_ERR_CUDA;
         if (!(sn.s3 = W.valid_buf()) || !(sn.sc = W.valid_buf()) || !(sn.sp = W.valid_buf())) return MFG_ERR_CUDA;
     }
     Snap& sn = snaps[0];
