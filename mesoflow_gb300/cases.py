@@ -455,13 +455,17 @@ class AmrCase:
 
 
 def catalyst_amr(n0=128, nlev=3, order=5, seed=4, blocking=16, max_grid=64, base_grid=32, u_in=1.0, dx0=1e-5,
-                 nspheres=80, nreact=8):
+                 nspheres=80, nreact=8, nested=True):
     """Catalyst block + spheres on 3 levels (ratio 2, base n0^3): level l+1
     covers the level-l cells within 2 cells of the immersed surface (cut cells
     and their neighbours), clustered into blocks of `blocking` cells and merged
     into uneven boxes of up to max_grid cells per side (a stand-in for AMReX's
     regrid, which is not vendored).  Chemistry, species and boundaries as
-    catalyst(): 8 gas + 2 site species, 8 Arrhenius surface reactions."""
+    catalyst(): 8 gas + 2 site species, 8 Arrhenius surface reactions.
+    nested: level l+1 keeps one block of level-l cells around it (inside the
+    domain), so that its ghost cells and their interpolation stencils lie on
+    level l (proper nesting, which the multi-level step needs when
+    blocking/2 >= 3)."""
     base = catalyst(n=8, order=order, seed=seed, nreact=nreact, u_in=u_in, dx=dx0)  # parameter tables only
     P = base.params
     L = n0 * dx0
@@ -498,6 +502,14 @@ def catalyst_amr(n0=128, nlev=3, order=5, seed=4, blocking=16, max_grid=64, base
             bz0, by0, bx0 = (2 * lo[2]) // blocking, (2 * lo[1]) // blocking, (2 * lo[0]) // blocking
             bz1, by1, bx1 = (2 * (hi[2] + 1)) // blocking, (2 * (hi[1] + 1)) // blocking, (2 * (hi[0] + 1)) // blocking
             inside[bz0:bz1, by0:by1, bx0:bx1] = True
+        if nested:  # erode the covered region by one block; outside the domain counts as covered
+            pad = np.pad(inside, 1, constant_values=True)
+            er = np.ones_like(inside)
+            for dz in (0, 1, 2):
+                for dy in (0, 1, 2):
+                    for dx_ in (0, 1, 2):
+                        er &= pad[dz:dz + nb, dy:dy + nb, dx_:dx_ + nb]
+            inside = er
         tag &= inside
         lev_boxes = _merge_blocks(tag, blocking, max_grid // blocking)
     # initial states: gas at rest except the inlet velocity in fluid cells, sites in solid cells
@@ -519,3 +531,30 @@ def catalyst_amr(n0=128, nlev=3, order=5, seed=4, blocking=16, max_grid=64, base
         states.append(state_from_prim(P, rho, u, zero, zero, np.full(shape, pres), spec, vf))
     meta = {"nlev": nlev, "per_level_boxes": [sum(1 for b in boxes if b[2] == l) for l in range(nlev)]}
     return AmrCase(P, geoms, boxes, states, meta)
+
+
+def two_level(case, fine_boxes, ratio=2):
+    """Two-level hierarchy over a single-level case: level 0 is the case's
+    boxes, level 1 the given boxes (inclusive fine-index corners, aligned to
+    the ratio), initialised by piecewise-constant injection of the coarse
+    state."""
+    g0 = case.geom
+    n = [g0.domain_hi[d] - g0.domain_lo[d] + 1 for d in range(3)]
+    prob_lo = [g0.prob_lo[d] for d in range(3)]
+    prob_hi = [g0.prob_lo[d] + n[d] * g0.dx[d] for d in range(3)]
+    per = [g0.is_periodic[d] for d in range(3)]
+    g1 = geometry((0, 0, 0), tuple(ratio * n[d] - 1 for d in range(3)), prob_lo, prob_hi, per)
+    boxes, states = [], []
+    for lo, hi in case.boxes:
+        boxes.append((tuple(lo), tuple(hi), 0))
+        states.append(np.ascontiguousarray(case.state[:, lo[2]:hi[2] + 1, lo[1]:hi[1] + 1, lo[0]:hi[0] + 1]))
+    for lo, hi in fine_boxes:
+        assert all(lo[d] % ratio == 0 and (hi[d] + 1) % ratio == 0 for d in range(3))
+        c = case.state[:, lo[2] // ratio:(hi[2] + 1) // ratio, lo[1] // ratio:(hi[1] + 1) // ratio,
+                       lo[0] // ratio:(hi[0] + 1) // ratio]
+        f = c.repeat(ratio, axis=1).repeat(ratio, axis=2).repeat(ratio, axis=3)
+        boxes.append((tuple(lo), tuple(hi), 1))
+        states.append(np.ascontiguousarray(f))
+    meta = dict(case.meta)
+    meta.update({"nlev": 2, "per_level_boxes": [len(case.boxes), len(fine_boxes)]})
+    return AmrCase(case.params, [g0, g1], boxes, states, meta)

@@ -164,14 +164,14 @@ class MultiLevel:
     """Boxes of several levels in one descriptor array (mfg_box.level set), for
     the batched entry points.  backend: 'numpy' or 'torch'."""
 
-    def __init__(self, amr, backend="torch", device=None):
+    def __init__(self, amr, backend="torch", device=None, with_dsdt=False):
         self.amr = amr
         self.ncomp = amr.ncomp
         self.levels = []
         self.index = []  # global box -> (level, local box)
         for l in range(len(amr.geoms)):
             bl = [(lo, hi) for lo, hi, lv in amr.boxes if lv == l]
-            self.levels.append(Level(bl, amr.ncomp, backend=backend, device=device, with_dsdt=False))
+            self.levels.append(Level(bl, amr.ncomp, backend=backend, device=device, with_dsdt=with_dsdt))
         counters = [0] * len(amr.geoms)
         for lo, hi, lv in amr.boxes:
             self.index.append((lv, counters[lv]))

@@ -4,6 +4,7 @@
 // restates mflo::Advance_coupled_strang and the step bookends.
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <vector>
 
 #include "mflo_oracle.hpp"
@@ -41,10 +42,13 @@ struct FluxFab {
     }
 };
 
-int dsdt_box(const Ctx& c, const mfg_geom* G, const mfg_box& b) {
+// keep (optional): receives the three face-flux FABs (the multi-level step's
+// flux registers read them).
+int dsdt_box(const Ctx& c, const mfg_geom* G, const mfg_box& b, FluxFab* keep = nullptr) {
     const int nc = ncomp_of(c.P);
     A4 phi(b.sborder), dsdt(b.dsdt);
-    FluxFab F[3];
+    FluxFab local[3];
+    FluxFab* F = keep ? keep : local;
     for (int d = 0; d < 3; d++) F[d].define(b, d, nc);
     for (int d = 0; d < 3; d++) {
         int hi[3] = {b.hi[0], b.hi[1], b.hi[2]};
@@ -141,13 +145,87 @@ inline bool odd_at_wall(int n) {  // Source/mflo.cpp:98-110
     return n == RHOU_INDX || n == RHOV_INDX || n == RHOW_INDX || n == VELX_INDX || n == VELY_INDX || n == VELZ_INDX;
 }
 
-int fill_patch(const Ctx& c, const Level& L, int s_src, double time) {
-    (void)time;
-    const mfg_geom* G = L.G;
+// Physical boundaries of the cells of [glo, ghi] that lie outside the domain
+// of G in non-periodic directions: faces, then edges, then corners, each from
+// the array itself (the rule of the comment above).
+int physbc_region(const Ctx& c, const mfg_geom* G, const A4& sb, const int glo[3], const int ghi[3]) {
     const mfg_params* P = c.P;
     const int nc = ncomp_of(P);
     const int* dlo = G->domain_lo;
     const int* dhi = G->domain_hi;
+    int status = MFG_OK;
+    for (int stage = 1; stage <= 3; stage++)
+        for (int k = glo[2]; k <= ghi[2]; k++)
+            for (int j = glo[1]; j <= ghi[1]; j++)
+                for (int i = glo[0]; i <= ghi[0]; i++) {
+                    int iv[3] = {i, j, k};
+                    bool outd[3];
+                    int nout = 0;
+                    for (int d = 0; d < 3; d++) {
+                        outd[d] = !G->is_periodic[d] && (iv[d] < dlo[d] || iv[d] > dhi[d]);
+                        nout += outd[d];
+                    }
+                    if (nout != stage) continue;
+                    int dstar = -1;
+                    for (int d = 0; d < 3; d++) {
+                        if (!outd[d]) continue;
+                        int kind = (iv[d] < dlo[d]) ? P->bc_lo[d] : P->bc_hi[d];
+                        if (kind == MFG_BC_EXT_DIR) dstar = d;
+                    }
+                    bool ext = dstar >= 0;
+                    if (!ext)
+                        for (int d = 0; d < 3; d++)
+                            if (outd[d]) dstar = d;
+                    bool lo_side = iv[dstar] < dlo[dstar];
+                    int kind = lo_side ? P->bc_lo[dstar] : P->bc_hi[dstar];
+                    int bnd = lo_side ? dlo[dstar] : dhi[dstar];
+                    int sv[3] = {i, j, k};
+                    if (ext) {
+                        sv[dstar] = bnd;
+                        double s_int[FLO_NVARS + MAXS], s_ext[FLO_NVARS + MAXS];
+                        for (int n = 0; n < nc; n++) s_int[n] = sb.at(sv, n);
+                        externalbc(c, lo_side ? P->ext_lo[dstar] : P->ext_hi[dstar], s_int, s_ext, dstar, lo_side ? +1 : -1);
+                        for (int n = 0; n < nc; n++) sb(i, j, k, n) = s_ext[n];
+                    } else if (kind == MFG_BC_FOEXTRAP) {
+                        sv[dstar] = bnd;
+                        for (int n = 0; n < nc; n++) sb(i, j, k, n) = sb.at(sv, n);
+                    } else if (kind == MFG_BC_WALL) {
+                        sv[dstar] = lo_side ? (2 * dlo[dstar] - iv[dstar] - 1) : (2 * dhi[dstar] - iv[dstar] + 1);
+                        for (int n = 0; n < nc; n++) sb(i, j, k, n) = odd_at_wall(n) ? -sb.at(sv, n) : sb.at(sv, n);
+                    } else {
+                        status = MFG_ERR_ARG;
+                    }
+                }
+    return status;
+}
+
+// Periodic image of iv inside the domain of G; false if iv lies outside in a
+// non-periodic direction.
+inline bool wrap_into(const mfg_geom* G, const int iv[3], int w[3]) {
+    bool inside = true;
+    for (int d = 0; d < 3; d++) {
+        const int len = G->domain_hi[d] - G->domain_lo[d] + 1;
+        w[d] = iv[d];
+        if (G->is_periodic[d]) {
+            while (w[d] < G->domain_lo[d]) w[d] += len;
+            while (w[d] > G->domain_hi[d]) w[d] -= len;
+        } else if (w[d] < G->domain_lo[d] || w[d] > G->domain_hi[d]) {
+            inside = false;
+        }
+    }
+    return inside;
+}
+
+int owner_of(const mfg_box* boxes, int nbox, const int w[3], int first = -1) {
+    if (first >= 0 && in_box(boxes[first], w[0], w[1], w[2])) return first;
+    for (int ob = 0; ob < nbox; ob++)
+        if (in_box(boxes[ob], w[0], w[1], w[2])) return ob;
+    return -1;
+}
+
+int fill_patch(const Ctx& c, const Level& L, int s_src, double time) {
+    (void)time;
+    const int nc = ncomp_of(c.P);
     int status = MFG_OK;
 #pragma omp parallel for schedule(dynamic)
     for (int ib = 0; ib < L.nbox; ib++) {
@@ -155,77 +233,24 @@ int fill_patch(const Ctx& c, const Level& L, int s_src, double time) {
         A4 sb(b.sborder);
         int glo[3], ghi[3];
         for (int d = 0; d < 3; d++) { glo[d] = b.lo[d] - MFG_NGROW; ghi[d] = b.hi[d] + MFG_NGROW; }
-        // 1) copy valid data (own box + other boxes + periodic images)
-        std::vector<signed char> nout;  // per grown cell: number of outside directions, -1 = filled
-        int n0 = ghi[0] - glo[0] + 1, n1 = ghi[1] - glo[1] + 1, n2 = ghi[2] - glo[2] + 1;
-        nout.assign((size_t)n0 * n1 * n2, 0);
+        // 1) copy valid data (own box + other boxes + periodic images); cells
+        //    not covered at this level stay unchanged
         for (int k = glo[2]; k <= ghi[2]; k++)
             for (int j = glo[1]; j <= ghi[1]; j++)
                 for (int i = glo[0]; i <= ghi[0]; i++) {
                     int iv[3] = {i, j, k}, w[3];
-                    int out = 0;
-                    for (int d = 0; d < 3; d++) {
-                        int len = dhi[d] - dlo[d] + 1;
-                        w[d] = iv[d];
-                        if (G->is_periodic[d]) {
-                            while (w[d] < dlo[d]) w[d] += len;
-                            while (w[d] > dhi[d]) w[d] -= len;
-                        } else if (w[d] < dlo[d] || w[d] > dhi[d]) {
-                            out++;
-                        }
-                    }
-                    size_t idx = (size_t)(i - glo[0]) + (size_t)(j - glo[1]) * n0 + (size_t)(k - glo[2]) * n0 * n1;
-                    if (out) { nout[idx] = (signed char)out; continue; }
-                    int src = -1;
-                    if (in_box(b, w[0], w[1], w[2])) src = ib;
-                    for (int ob = 0; src < 0 && ob < L.nbox; ob++)
-                        if (in_box(L.boxes[ob], w[0], w[1], w[2])) src = ob;
-                    nout[idx] = -1;
-                    if (src < 0) continue;  // not covered at this level (unchanged)
+                    if (!wrap_into(L.G, iv, w)) continue;
+                    const int src = owner_of(L.boxes, L.nbox, w, ib);
+                    if (src < 0) continue;
                     A4 s(s_src ? L.boxes[src].s_new : L.boxes[src].s_old);
                     for (int n = 0; n < nc; n++) sb(i, j, k, n) = s(w[0], w[1], w[2], n);
                 }
         // 2) physical boundaries: faces, then edges, then corners
-        for (int stage = 1; stage <= 3; stage++)
-            for (int k = glo[2]; k <= ghi[2]; k++)
-                for (int j = glo[1]; j <= ghi[1]; j++)
-                    for (int i = glo[0]; i <= ghi[0]; i++) {
-                        size_t idx = (size_t)(i - glo[0]) + (size_t)(j - glo[1]) * n0 + (size_t)(k - glo[2]) * n0 * n1;
-                        if (nout[idx] != stage) continue;
-                        int iv[3] = {i, j, k};
-                        bool outd[3];
-                        for (int d = 0; d < 3; d++) outd[d] = !G->is_periodic[d] && (iv[d] < dlo[d] || iv[d] > dhi[d]);
-                        int dstar = -1;
-                        for (int d = 0; d < 3; d++) {
-                            if (!outd[d]) continue;
-                            int kind = (iv[d] < dlo[d]) ? P->bc_lo[d] : P->bc_hi[d];
-                            if (kind == MFG_BC_EXT_DIR) dstar = d;
-                        }
-                        bool ext = dstar >= 0;
-                        if (!ext)
-                            for (int d = 0; d < 3; d++)
-                                if (outd[d]) dstar = d;
-                        bool lo_side = iv[dstar] < dlo[dstar];
-                        int kind = lo_side ? P->bc_lo[dstar] : P->bc_hi[dstar];
-                        int bnd = lo_side ? dlo[dstar] : dhi[dstar];
-                        int sv[3] = {i, j, k};
-                        if (ext) {
-                            sv[dstar] = bnd;
-                            double s_int[FLO_NVARS + MAXS], s_ext[FLO_NVARS + MAXS];
-                            for (int n = 0; n < nc; n++) s_int[n] = sb.at(sv, n);
-                            externalbc(c, lo_side ? P->ext_lo[dstar] : P->ext_hi[dstar], s_int, s_ext, dstar, lo_side ? +1 : -1);
-                            for (int n = 0; n < nc; n++) sb(i, j, k, n) = s_ext[n];
-                        } else if (kind == MFG_BC_FOEXTRAP) {
-                            sv[dstar] = bnd;
-                            for (int n = 0; n < nc; n++) sb(i, j, k, n) = sb.at(sv, n);
-                        } else if (kind == MFG_BC_WALL) {
-                            sv[dstar] = lo_side ? (2 * dlo[dstar] - iv[dstar] - 1) : (2 * dhi[dstar] - iv[dstar] + 1);
-                            for (int n = 0; n < nc; n++) sb(i, j, k, n) = odd_at_wall(n) ? -sb.at(sv, n) : sb.at(sv, n);
-                        } else {
+        const int rc = physbc_region(c, L.G, sb, glo, ghi);
+        if (rc) {
 #pragma omp critical
-                            status = MFG_ERR_ARG;
-                        }
-                    }
+            status = rc;
+        }
     }
     return status;
 }
@@ -430,6 +455,366 @@ double est_timestep(const Ctx& c, const Level& L) {  // mflo_timestep.cpp:53-153
     return dt_est;
 }
 
+// ---- multi-level step ------------------------------------------------------
+// mflo::timeStep / Advance_coupled_strang (Source/mflo_evolve.cpp:174-311)
+// with the AMReX pieces they call, restated from AMReX's published semantics
+// (AMReX is not vendored in the reference, so this part is unpinned):
+//  * GetData (Source/mflo.cpp:310-330): data at `time` is phi_new or phi_old
+//    when within 1e-3 dt of t_new / t_old, else the two in linear
+//    combination (t1-time)/(t1-t0) old + (time-t0)/(t1-t0) new
+//    (FillPatchSingleLevel with two time levels);
+//  * FillPatchTwoLevels (Source/mflo_gridwork.cpp:135-173): ghost cells of a
+//    fine box that lie inside the (periodically extended) domain and are not
+//    covered by the fine level are interpolated with cell_cons_interp from a
+//    coarse patch (the coarsened grown box, grown by one) filled from the
+//    coarse level at `time` plus the coarse physical boundaries; then the fine
+//    level's valid data is copied and the fine physical boundaries applied;
+//  * cell_cons_interp = CellConservativeLinear without cross-component
+//    limiting: per component MC-limited central slopes (one-sided 4-point
+//    slopes at ext_dir domain faces), scaled by one factor per coarse cell and
+//    component that keeps every fine value within the 27-neighbour coarse
+//    bounds, fine = crse + sum_d off_d slope_d;
+//  * FluxRegister: CrseInit(ADD) adds scale x coarse flux, FineAdd adds
+//    scale x each of the ratio^2 fine faces (higher transverse direction
+//    outer), Reflux visits the orientations x-lo, y-lo, z-lo, x-hi, y-hi,
+//    z-hi and adds -reg/vol (lo) or +reg/vol (hi) to the coarse cell outside
+//    the fine box (registers whose outside cell is covered by the fine level
+//    or lies outside the domain change nothing that average_down keeps);
+//  * average_down: covered coarse cell = (1/ratio^3) x the sum of its fine
+//    cells (k, j, i order), every component.
+inline int floor_div(int a, int r) { return a >= 0 ? a / r : -((-a + r - 1) / r); }
+
+struct RegEnt {
+    int fb, cb, d, side;
+    int cc[3], cf[3], ff[3];
+    std::vector<double> v;
+};
+
+struct Amr {
+    const mfg_params* P;
+    Ctx c;
+    int nlev, nc;
+    std::vector<const mfg_geom*> G;
+    std::vector<int> ratio;                    // to the coarser level ([0] = 1)
+    std::vector<std::vector<mfg_box>> lv;      // boxes per level
+    std::vector<std::vector<std::array<FluxFab, 3>>> flux;
+    std::vector<std::vector<RegEnt>> reg;      // [l]: registers of the l / l-1 interface
+    std::vector<double> t_old, t_new, dt;
+    bool only_flow;
+};
+
+// cell_cons_interp of component n at fine cell (i, j, k) from the coarse patch u.
+double cc_interp(const Amr& A, int l, const A4& u, const int cplo[3], const int cphi[3], int i, int j, int k, int n) {
+    const mfg_params* P = A.P;
+    const mfg_geom* Gc = A.G[l - 1];
+    const int r = A.ratio[l];
+    const int ic[3] = {floor_div(i, r), floor_div(j, r), floor_div(k, r)};
+    const int fv[3] = {i, j, k};
+    auto U = [&](int d, int o) {
+        int q[3] = {ic[0], ic[1], ic[2]};
+        q[d] += o;
+        return u(q[0], q[1], q[2], n);
+    };
+    const double u0 = u(ic[0], ic[1], ic[2], n);
+    double sl[3];
+    for (int d = 0; d < 3; d++) {
+        double dc = 0.5 * (U(d, 1) - U(d, -1));
+        if (!Gc->is_periodic[d] && ic[d] == Gc->domain_lo[d] && P->bc_lo[d] == MFG_BC_EXT_DIR) {
+            if (ic[d] + 2 <= cphi[d])
+                dc = -16. / 15. * U(d, -1) + 0.5 * u0 + 2. / 3. * U(d, 1) - 0.1 * U(d, 2);
+            else
+                dc = 0.25 * (U(d, 1) + 5. * u0 - 6. * U(d, -1));
+        }
+        if (!Gc->is_periodic[d] && ic[d] == Gc->domain_hi[d] && P->bc_hi[d] == MFG_BC_EXT_DIR) {
+            if (ic[d] - 2 >= cplo[d])
+                dc = 16. / 15. * U(d, 1) - 0.5 * u0 - 2. / 3. * U(d, -1) + 0.1 * U(d, -2);
+            else
+                dc = -0.25 * (U(d, -1) + 5. * u0 - 6. * U(d, 1));
+        }
+        const double df = 2.0 * (U(d, 1) - u0);
+        const double db = 2.0 * (u0 - U(d, -1));
+        double sx = (df * db >= 0.0) ? std::min(std::fabs(df), std::fabs(db)) : 0.0;
+        sx = std::copysign(1.0, dc) * std::min(sx, std::fabs(dc));
+        sl[d] = sx;
+    }
+    double alpha = 1.0;
+    if (sl[0] != 0.0 || sl[1] != 0.0 || sl[2] != 0.0) {
+        const double f = (double)(r - 1);
+        const double g = (double)(2 * r);
+        const double dumax = std::fabs(sl[0]) * f / g + std::fabs(sl[1]) * f / g + std::fabs(sl[2]) * f / g;
+        double umax = u0, umin = u0;
+        for (int kk = -1; kk <= 1; kk++)
+            for (int jj = -1; jj <= 1; jj++)
+                for (int ii = -1; ii <= 1; ii++) {
+                    const double x = u(ic[0] + ii, ic[1] + jj, ic[2] + kk, n);
+                    umin = std::min(umin, x);
+                    umax = std::max(umax, x);
+                }
+        if (dumax * alpha > (umax - u0)) alpha = (umax - u0) / dumax;
+        if (dumax * alpha > (u0 - umin)) alpha = (u0 - umin) / dumax;
+    }
+    double off[3];
+    for (int d = 0; d < 3; d++) off[d] = (fv[d] - ic[d] * r + 0.5) / (double)r - 0.5;
+    return u0 + off[0] * (sl[0] * alpha) + off[1] * (sl[1] * alpha) + off[2] * (sl[2] * alpha);
+}
+
+// Data of level l at time T: 0 old, 1 new, 2 a*old + b*new.
+int get_data(const Amr& A, int l, double T, double& a, double& b) {
+    const double teps = (A.t_new[l] - A.t_old[l]) * 1.e-3;
+    if (T > A.t_new[l] - teps && T < A.t_new[l] + teps) return 1;
+    if (T > A.t_old[l] - teps && T < A.t_old[l] + teps) return 0;
+    const double t0 = A.t_old[l], t1 = A.t_new[l];
+    a = (t1 - T) / (t1 - t0);
+    b = (T - t0) / (t1 - t0);
+    return 2;
+}
+
+int fill_level(Amr& A, int l, int s_src, double T) {
+    const int nc = A.nc;
+    std::vector<mfg_box>& bl = A.lv[l];
+    const int nb = (int)bl.size();
+    double ca = 0.0, cb = 0.0;
+    const int ckind = l > 0 ? get_data(A, l - 1, T, ca, cb) : 0;
+    int status = MFG_OK;
+#pragma omp parallel for schedule(dynamic)
+    for (int ib = 0; ib < nb; ib++) {
+        const mfg_box& b = bl[ib];
+        A4 sb(b.sborder);
+        int glo[3], ghi[3];
+        for (int d = 0; d < 3; d++) { glo[d] = b.lo[d] - MFG_NGROW; ghi[d] = b.hi[d] + MFG_NGROW; }
+        std::vector<double> cpv;
+        A4 cp;
+        int clo[3] = {0, 0, 0}, chi[3] = {0, 0, 0};
+        int rc = MFG_OK;
+        if (l > 0) {  // coarse patch at time T
+            const int r = A.ratio[l];
+            const std::vector<mfg_box>& cl = A.lv[l - 1];
+            size_t len[3];
+            for (int d = 0; d < 3; d++) {
+                clo[d] = floor_div(glo[d], r) - 1;
+                chi[d] = floor_div(ghi[d], r) + 1;
+                len[d] = (size_t)(chi[d] - clo[d] + 1);
+            }
+            cpv.assign(len[0] * len[1] * len[2] * nc, 0.0);
+            cp.p = cpv.data();
+            cp.js = (int64_t)len[0];
+            cp.ks = (int64_t)(len[0] * len[1]);
+            cp.ns = (int64_t)(len[0] * len[1] * len[2]);
+            cp.b0 = clo[0]; cp.b1 = clo[1]; cp.b2 = clo[2];
+            int hint = -1;
+            for (int k = clo[2]; k <= chi[2]; k++)
+                for (int j = clo[1]; j <= chi[1]; j++)
+                    for (int i = clo[0]; i <= chi[0]; i++) {
+                        int iv[3] = {i, j, k}, w[3];
+                        if (!wrap_into(A.G[l - 1], iv, w)) continue;
+                        const int src = owner_of(cl.data(), (int)cl.size(), w, hint);
+                        if (src < 0) { rc = MFG_ERR_ARG; continue; }  // not properly nested
+                        hint = src;
+                        A4 so(cl[src].s_old), sn(cl[src].s_new);
+                        for (int n = 0; n < nc; n++) {
+                            const double x0 = so(w[0], w[1], w[2], n), x1 = sn(w[0], w[1], w[2], n);
+                            cp(i, j, k, n) = ckind == 0 ? x0 : ckind == 1 ? x1 : ca * x0 + cb * x1;
+                        }
+                    }
+            const int r2 = physbc_region(A.c, A.G[l - 1], cp, clo, chi);
+            if (r2) rc = r2;
+        }
+        int hint = ib;
+        for (int k = glo[2]; k <= ghi[2]; k++)
+            for (int j = glo[1]; j <= ghi[1]; j++)
+                for (int i = glo[0]; i <= ghi[0]; i++) {
+                    int iv[3] = {i, j, k}, w[3];
+                    if (!wrap_into(A.G[l], iv, w)) continue;
+                    const int src = owner_of(bl.data(), nb, w, hint);
+                    if (src >= 0) {
+                        hint = src;
+                        A4 s(s_src ? bl[src].s_new : bl[src].s_old);
+                        for (int n = 0; n < nc; n++) sb(i, j, k, n) = s(w[0], w[1], w[2], n);
+                    } else if (l > 0) {
+                        for (int n = 0; n < nc; n++) sb(i, j, k, n) = cc_interp(A, l, cp, clo, chi, i, j, k, n);
+                    }
+                }
+        const int r3 = physbc_region(A.c, A.G[l], sb, glo, ghi);
+        if (r3) rc = r3;
+        if (rc) {
+#pragma omp critical
+            status = rc;
+        }
+    }
+    return status;
+}
+
+// Registers of the interface between level l (fine) and l-1.
+int build_registers(Amr& A, int l) {
+    const int r = A.ratio[l];
+    const mfg_geom* Gc = A.G[l - 1];
+    const std::vector<mfg_box>& fl = A.lv[l];
+    const std::vector<mfg_box>& cl = A.lv[l - 1];
+    A.reg[l].clear();
+    for (int side = 0; side < 2; side++)
+        for (int d = 0; d < 3; d++)
+            for (int fb = 0; fb < (int)fl.size(); fb++) {
+                const mfg_box& b = fl[fb];
+                const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+                const int fface = side ? b.hi[d] + 1 : b.lo[d];
+                const int cface = fface / r;
+                for (int q2 = b.lo[t2] / r; q2 <= (b.hi[t2] + 1) / r - 1; q2++)
+                    for (int q1 = b.lo[t1] / r; q1 <= (b.hi[t1] + 1) / r - 1; q1++) {
+                        int cc[3];
+                        cc[d] = side ? cface : cface - 1;
+                        cc[t1] = q1;
+                        cc[t2] = q2;
+                        int w[3];
+                        if (!wrap_into(Gc, cc, w)) continue;
+                        const int fw[3] = {w[0] * r, w[1] * r, w[2] * r};
+                        if (owner_of(fl.data(), (int)fl.size(), fw) >= 0) continue;  // covered
+                        const int cb = owner_of(cl.data(), (int)cl.size(), w);
+                        if (cb < 0) return MFG_ERR_ARG;
+                        RegEnt e;
+                        e.fb = fb;
+                        e.cb = cb;
+                        e.d = d;
+                        e.side = side;
+                        for (int q = 0; q < 3; q++) { e.cc[q] = w[q]; e.cf[q] = w[q]; }
+                        e.cf[d] = side ? w[d] : w[d] + 1;
+                        e.ff[d] = fface;
+                        e.ff[t1] = q1 * r;
+                        e.ff[t2] = q2 * r;
+                        e.v.assign(A.nc, 0.0);
+                        A.reg[l].push_back(std::move(e));
+                    }
+            }
+    return MFG_OK;
+}
+
+void reg_zero(Amr& A, int l) {
+    for (RegEnt& e : A.reg[l]) std::fill(e.v.begin(), e.v.end(), 0.0);
+}
+
+void reg_crse(Amr& A, int l, const double scale[3]) {  // registers of l+1 from level l's fluxes
+    for (RegEnt& e : A.reg[l + 1]) {
+        const A4& F = A.flux[l][e.cb][e.d].a;
+        for (int n = 0; n < A.nc; n++) e.v[n] = e.v[n] + F(e.cf[0], e.cf[1], e.cf[2], n) * scale[e.d];
+    }
+}
+
+void reg_fine(Amr& A, int l, const double scale[3]) {  // registers of l from level l's fluxes
+    const int r = A.ratio[l];
+    for (RegEnt& e : A.reg[l]) {
+        const A4& F = A.flux[l][e.fb][e.d].a;
+        const int t1 = e.d == 0 ? 1 : 0, t2 = e.d == 2 ? 1 : 2;
+        for (int n = 0; n < A.nc; n++)
+            for (int o2 = 0; o2 < r; o2++)
+                for (int o1 = 0; o1 < r; o1++) {
+                    int q[3] = {e.ff[0], e.ff[1], e.ff[2]};
+                    q[t1] += o1;
+                    q[t2] += o2;
+                    e.v[n] = e.v[n] + scale[e.d] * F(q[0], q[1], q[2], n);
+                }
+    }
+}
+
+void reflux(Amr& A, int l) {  // level l from the registers of l+1
+    const double* dx = A.G[l]->dx;
+    const double vol = dx[0] * dx[1] * dx[2];
+    for (int o = 0; o < 6; o++)
+        for (RegEnt& e : A.reg[l + 1]) {
+            if (e.d + 3 * e.side != o) continue;
+            A4 s(A.lv[l][e.cb].s_new);
+            for (int n = 0; n < A.nc; n++) {
+                double& x = s(e.cc[0], e.cc[1], e.cc[2], n);
+                x += e.side ? (1.0 * e.v[n]) / vol : (-1.0 * e.v[n]) / vol;
+            }
+        }
+}
+
+int average_down(Amr& A, int l) {  // level l+1 onto level l
+    const int r = A.ratio[l + 1];
+    const double volfrac = 1.0 / (double)(r * r * r);
+    const std::vector<mfg_box>& cl = A.lv[l];
+    for (const mfg_box& b : A.lv[l + 1]) {
+        A4 f(b.s_new);
+        for (int k = b.lo[2] / r; k <= (b.hi[2] + 1) / r - 1; k++)
+            for (int j = b.lo[1] / r; j <= (b.hi[1] + 1) / r - 1; j++)
+                for (int i = b.lo[0] / r; i <= (b.hi[0] + 1) / r - 1; i++) {
+                    const int w[3] = {i, j, k};
+                    const int cb = owner_of(cl.data(), (int)cl.size(), w);
+                    if (cb < 0) return MFG_ERR_ARG;
+                    A4 s(cl[cb].s_new);
+                    for (int n = 0; n < A.nc; n++) {
+                        double c = 0.;
+                        for (int kr = 0; kr < r; kr++)
+                            for (int jr = 0; jr < r; jr++)
+                                for (int ir = 0; ir < r; ir++) c += f(i * r + ir, j * r + jr, k * r + kr, n);
+                        s(i, j, k, n) = volfrac * c;
+                    }
+                }
+    }
+    return MFG_OK;
+}
+
+int amr_advance(Amr& A, int l, double time, double dtl) {
+    std::vector<mfg_box>& bl = A.lv[l];
+    const int nb = (int)bl.size();
+    for (int ib = 0; ib < nb; ib++) copy_valid(bl[ib], bl[ib].s_old, bl[ib].s_new, A.nc);  // swap
+    A.t_old[l] = A.t_new[l];
+    A.t_new[l] += dtl;
+    if (l + 1 < A.nlev) reg_zero(A, l + 1);
+    const double* dx = A.G[l]->dx;
+    const double dA[3] = {dx[1] * dx[2], dx[0] * dx[2], dx[0] * dx[1]};
+    Level L{A.P, A.G[l], bl.data(), nb};
+    for (int stage = 1; stage <= 3; stage++) {
+        int rc = fill_level(A, l, stage == 1 ? 0 : 1, stage == 1 ? time : time + dtl);
+        if (rc) return rc;
+#pragma omp parallel for schedule(dynamic)
+        for (int ib = 0; ib < nb; ib++) {
+            const mfg_box& b = bl[ib];
+            A4 phi(b.sborder);
+            for (int k = b.lo[2]; k <= b.hi[2]; k++)
+                for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                    for (int i = b.lo[0]; i <= b.hi[0]; i++) update_cutcells(A.c, i, j, k, phi, dx);
+        }
+        int st = MFG_OK;
+#pragma omp parallel for schedule(dynamic)
+        for (int ib = 0; ib < nb; ib++) {
+            int r = dsdt_box(A.c, A.G[l], bl[ib], A.flux[l][ib].data());
+            if (r) {
+#pragma omp critical
+                st = r;
+            }
+        }
+        if (st) return st;
+        for (int ib = 0; ib < nb; ib++) stage_algebra(A.c, bl[ib], stage, dtl);
+        const double ff = stage < 3 ? sixth : two3rd;
+        if (l + 1 < A.nlev) {
+            const double sc[3] = {-dtl * dA[0] * ff, -dtl * dA[1] * ff, -dtl * dA[2] * ff};
+            reg_crse(A, l, sc);
+        }
+        if (l > 0) {
+            const double sc[3] = {dtl * dA[0] * ff, dtl * dA[1] * ff, dtl * dA[2] * ff};
+            reg_fine(A, l, sc);
+        }
+    }
+    if (!A.only_flow) {
+        for (int ib = 0; ib < nb; ib++) copy_valid(bl[ib], bl[ib].s_old, bl[ib].s_new, A.nc);  // swap
+        int rc = chem_substep(A.c, L, dtl);
+        if (rc) return rc;
+    }
+    return MFG_OK;
+}
+
+int amr_time_step(Amr& A, int l, double time) {
+    int rc = amr_advance(A, l, time, A.dt[l]);
+    if (rc) return rc;
+    if (l + 1 < A.nlev) {
+        for (int i = 1; i <= A.ratio[l + 1]; i++)
+            if ((rc = amr_time_step(A, l + 1, time + (i - 1) * A.dt[l + 1]))) return rc;
+        reflux(A, l);
+        if ((rc = average_down(A, l))) return rc;
+    }
+    return MFG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -568,6 +953,62 @@ int oracle_advance(const mfg_params* P, const mfg_geom* G, const mfg_box* boxes,
     if (rc) return rc;
     if (clip) clip_species(c, L);
     if (resnorms) residual_norms(c, L, dt, resnorms);
+    return MFG_OK;
+}
+
+// One coarse step of a multi-level run: the step body of mflo::EvolveAMR
+// (Source/mflo_evolve.cpp:26-58) around timeStep's subcycling (:174-247):
+// level l advances with dt0 / (ratio_1 ... ratio_l), its face fluxes feed the
+// flux registers of both of its interfaces, and after the substeps of the
+// finer level it is refluxed and averaged down onto; then the primitive
+// refresh and species clipping of every level.  boxes[].level selects the
+// level; geoms holds one geometry per level (ratio = dx[l-1] / dx[l]); fine
+// boxes must be aligned to the ratio and properly nested (MFG_ERR_ARG
+// otherwise).  On exit s_new holds the new state and s_old phi_old.
+int oracle_advance_amr(const mfg_params* P, const mfg_geom* geoms, const mfg_box* boxes, int nbox, int nlev,
+                       double time, double dt0, int only_flow, int clip) {
+    if (nlev < 1) return MFG_ERR_ARG;
+    Amr A;
+    A.P = P;
+    A.c = Ctx{P, P->nspec};
+    A.nlev = nlev;
+    A.nc = ncomp_of(P);
+    A.only_flow = only_flow != 0;
+    A.G.resize(nlev);
+    A.ratio.assign(nlev, 1);
+    A.lv.resize(nlev);
+    A.flux.resize(nlev);
+    A.reg.resize(nlev);
+    for (int l = 0; l < nlev; l++) {
+        A.G[l] = &geoms[l];
+        if (l > 0) {
+            A.ratio[l] = (int)(geoms[l - 1].dx[0] / geoms[l].dx[0] + 0.5);
+            if (A.ratio[l] < 2) return MFG_ERR_ARG;
+        }
+    }
+    for (int b = 0; b < nbox; b++) {
+        const int l = boxes[b].level;
+        if (l < 0 || l >= nlev) return MFG_ERR_ARG;
+        for (int d = 0; d < 3; d++)
+            if (l > 0 && (floor_div(boxes[b].lo[d], A.ratio[l]) * A.ratio[l] != boxes[b].lo[d] ||
+                          floor_div(boxes[b].hi[d] + 1, A.ratio[l]) * A.ratio[l] != boxes[b].hi[d] + 1))
+                return MFG_ERR_ARG;
+        A.lv[l].push_back(boxes[b]);
+    }
+    for (int l = 0; l < nlev; l++) A.flux[l].resize(A.lv[l].size());
+    A.t_old.assign(nlev, time);
+    A.t_new.assign(nlev, time);
+    A.dt.assign(nlev, dt0);
+    for (int l = 1; l < nlev; l++) A.dt[l] = A.dt[l - 1] / A.ratio[l];
+    int rc;
+    for (int l = 1; l < nlev; l++)
+        if ((rc = build_registers(A, l))) return rc;
+    if ((rc = amr_time_step(A, 0, time))) return rc;
+    for (int l = 0; l < nlev; l++) {
+        Level L{P, &geoms[l], A.lv[l].data(), (int)A.lv[l].size()};
+        if ((rc = update_prims(A.c, L))) return rc;
+        if (clip) clip_species(A.c, L);
+    }
     return MFG_OK;
 }
 

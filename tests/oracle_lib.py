@@ -33,6 +33,7 @@ def load(variant="strict"):
         "oracle_residual_norms": [PP, BP, C.c_int, C.c_double, C.POINTER(C.c_double)],
         "oracle_est_timestep": [PP, GP, BP, C.c_int, C.POINTER(C.c_double)],
         "oracle_advance": [PP, GP, BP, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)],
+        "oracle_advance_amr": [PP, GP, BP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int],
         "oracle_abi_layout": [C.POINTER(C.c_int64), C.c_int],
         "oracle_objective": [PP, GP, BP, C.c_int, C.POINTER(C.c_double)],
     }

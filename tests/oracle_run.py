@@ -43,3 +43,54 @@ class OracleLevel:
 
     def state(self):
         return self.level.get_state(self.case.shape_zyx)
+
+
+class OracleAmr:
+    """Multi-level runs of the oracle (subcycled coarse steps with flux
+    registers, reflux and average-down) on an AmrCase, in host memory."""
+
+    def __init__(self, amr, variant="strict"):
+        from mesoflow_gb300.level import MultiLevel
+        self.lib = oracle_lib.load(variant)
+        self.amr = amr
+        self.ml = MultiLevel(amr, backend="numpy", with_dsdt=True)
+        self.desc = self.ml.descriptors()
+        self.geoms = self.ml.geoms()
+        self.time = 0.0
+
+    def advance(self, dt0, only_flow=False, clip=True):
+        rc = self.lib.oracle_advance_amr(C.byref(self.amr.params), self.geoms, self.desc, len(self.amr.boxes),
+                                         len(self.amr.geoms), self.time, dt0, int(only_flow), int(clip))
+        if rc != 0:
+            raise abi.MfloError("oracle_advance_amr", rc)
+        self.time += dt0
+
+    def box_state(self, g):
+        return self.ml.box_state(g)
+
+    def composite_totals(self, comps):
+        """Sum over the finest data covering each point: level-l cells covered
+        by level l+1 are left out; each level weighted by its cell volume."""
+        amr = self.amr
+        tot = np.zeros(len(comps))
+        mag = np.zeros(len(comps))
+        nlev = len(amr.geoms)
+        for g, (lo, hi, lv) in enumerate(amr.boxes):
+            s = self.box_state(g)
+            mask = np.ones(s.shape[1:], dtype=bool)
+            if lv + 1 < nlev:
+                r = int(round(amr.geoms[lv].dx[0] / amr.geoms[lv + 1].dx[0]))
+                for flo, fhi, fl in amr.boxes:
+                    if fl != lv + 1:
+                        continue
+                    a = [max(lo[d], flo[d] // r) for d in range(3)]
+                    b = [min(hi[d], (fhi[d] + 1) // r - 1) for d in range(3)]
+                    if all(a[d] <= b[d] for d in range(3)):
+                        mask[a[2] - lo[2]:b[2] - lo[2] + 1, a[1] - lo[1]:b[1] - lo[1] + 1,
+                             a[0] - lo[0]:b[0] - lo[0] + 1] = False
+            gm = amr.geoms[lv]
+            vol = gm.dx[0] * gm.dx[1] * gm.dx[2]
+            for q, c in enumerate(comps):
+                tot[q] += s[c][mask].sum(dtype=np.float64) * vol
+                mag[q] += np.abs(s[c][mask]).sum(dtype=np.float64) * vol
+        return tot, mag
