@@ -173,7 +173,11 @@ def algorithmic(kind, case, a, nlaunch_per_step):
 def run_amr(a):
     """Batched AMR form vs plain per-box launches of the same kernels on the
     3-level catalyst hierarchy (base 128^3, ratio 2, ~1400 uneven boxes of
-    16-64 cells, 8 gas + 2 site species, 8 Arrhenius surface reactions, WENO5)."""
+    16-64 cells, properly nested, 8 gas + 2 site species, 8 Arrhenius surface
+    reactions, WENO5).  Headline: the reference's multi-level coarse step
+    (levels subcycled, two-level fill with conservative interpolation, flux
+    registers, reflux, average-down); also the common-dt form of the same
+    hierarchy.  A cell-update is one cell advanced one step of its level."""
     import torch
     from mesoflow_gb300 import abi, cases
     from mesoflow_gb300.level import MultiLevel
@@ -188,39 +192,70 @@ def run_amr(a):
     s = torch.cuda.Stream()
     st = C.c_void_p(s.cuda_stream)
     cells = lib.mfg_boxlist_cells(h)
-    dt = 1e-9
-    res = {}
+    nlev = len(amr.geoms)
+    lev_cells = [0] * nlev
+    for lo, hi, lv in amr.boxes:
+        lev_cells[lv] += int(np.prod([hi[d] - lo[d] + 1 for d in range(3)]))
+    dt0 = 4e-9                                           # coarse step; finest level 1e-9
+    updates_amr = sum(c * 2 ** l for l, c in enumerate(lev_cells))
     tune = (C.c_double * 16)()
-    for name, mode in (("plain_per_box", 0), ("batched", 1), ("batched_graph", 2)):
-        if mode == 1:
-            with torch.cuda.stream(s):
-                abi.check("mfg_boxlist_autotune", lib.mfg_boxlist_autotune(h, dt, tune, st))
-            ml.set_states(amr.states)
+    with torch.cuda.stream(s):
+        abi.check("mfg_boxlist_autotune", lib.mfg_boxlist_autotune(h, dt0 / 4, tune, st))
+    ml.set_states(amr.states)
+
+    def timed(fn, mode):
         with torch.cuda.stream(s):
             for _ in range(a.warmup):
-                abi.check("mfg_boxlist_step", lib.mfg_boxlist_step(h, 0.0, dt, mode, st))
+                abi.check("step", fn(h, 0.0, mode))
             torch.cuda.synchronize()
             l0 = lib.mfg_launch_count()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(s)
             for _ in range(a.steps):
-                abi.check("mfg_boxlist_step", lib.mfg_boxlist_step(h, 0.0, dt, mode, st))
+                abi.check("step", fn(h, 0.0, mode))
             e1.record(s)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / a.steps
-        res[name] = {"ms_per_step": ms, "value": cells / (ms / 1e3),
-                     "host_launches_per_step": (lib.mfg_launch_count() - l0) / a.steps}
+        return e0.elapsed_time(e1) / a.steps, (lib.mfg_launch_count() - l0) / a.steps
+
+    def sub_step(hh, t, mode):
+        return lib.mfg_boxlist_step_amr(hh, t, dt0, mode, st)
+
+    def common_step(hh, t, mode):
+        return lib.mfg_boxlist_step(hh, t, dt0 / 4, mode, st)
+
+    res = {}
+    for form, fn, upd in (("subcycled", sub_step, updates_amr), ("common_dt", common_step, cells)):
+        for name, mode in (("plain_per_box", 0), ("batched", 1), ("batched_graph", 2)):
+            ms, launches = timed(fn, mode)
+            res.setdefault(form, {})[name] = {"ms_per_step": ms, "value": upd / (ms / 1e3),
+                                              "host_launches_per_step": launches}
+    # per-kernel-kind time of one batched subcycled step (CUDA events per launch)
+    lib.mfg_profile(1)
+    with torch.cuda.stream(s):
+        abi.check("step", sub_step(h, 0.0, 1))
+    torch.cuda.synchronize()
+    kk = 32
+    kms, kcnt = (C.c_double * kk)(), (C.c_longlong * kk)()
+    nk = lib.mfg_profile_read(kms, kcnt, kk)
+    lib.mfg_profile(0)
+    kernels = {lib.mfg_profile_name(i).decode(): {"ms": kms[i], "launches": kcnt[i]} for i in range(nk) if kcnt[i]}
     lib.mfg_boxlist_destroy(h)
     phases = ["fill", "cut", "face", "flux", "update"]
+    sub = res["subcycled"]
     out = {"metric": "RK3 cell-updates/s (FP64 3-level AMR, batched vs plain)", "unit": UNIT,
-           "value": res["batched_graph"]["value"], "higher_is_better": True, "n_gpus": 1, "steps": a.steps,
+           "value": sub["batched_graph"]["value"], "higher_is_better": True, "n_gpus": 1, "steps": a.steps,
            "warmup": a.warmup, "dtype": "f64", "data": "synthetic",
            "config": {"workload": "catalyst block + 80 seeded spheres, 3 levels ratio 2, base 128^3, "
-                                  f"{len(amr.boxes)} boxes {amr.meta['per_level_boxes']}, cells {cells}, "
-                                  "8 gas + 2 site species, 8 Arrhenius surface reactions, order_hyp 5, common dt"},
-           "modes": res,
-           "speedup_batched_graph_vs_plain": res["plain_per_box"]["ms_per_step"] / res["batched_graph"]["ms_per_step"],
-           "speedup_batched_vs_plain": res["plain_per_box"]["ms_per_step"] / res["batched"]["ms_per_step"],
+                                  f"{len(amr.boxes)} boxes {amr.meta['per_level_boxes']}, cells {lev_cells}, "
+                                  "8 gas + 2 site species, 8 Arrhenius surface reactions, order_hyp 5, "
+                                  f"subcycled coarse step dt0 {dt0} (cell-updates per coarse step "
+                                  f"{updates_amr}), flux registers, reflux, average-down"},
+           "modes": sub,
+           "speedup_batched_graph_vs_plain": sub["plain_per_box"]["ms_per_step"] / sub["batched_graph"]["ms_per_step"],
+           "speedup_batched_vs_plain": sub["plain_per_box"]["ms_per_step"] / sub["batched"]["ms_per_step"],
+           "common_dt": dict(res["common_dt"], speedup_batched_graph_vs_plain=(
+               res["common_dt"]["plain_per_box"]["ms_per_step"] / res["common_dt"]["batched_graph"]["ms_per_step"])),
+           "kernels_subcycled_batched": kernels,
            "autotune": {p: {"tile_items": tune[3 * i], "grid": tune[3 * i + 1], "ms": tune[3 * i + 2]}
                         for i, p in enumerate(phases)},
            "flux_form": {2: "column sweep", 1: "WENO5 per face", 0: "generic"}.get(int(tune[15]), "?")}

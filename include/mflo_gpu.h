@@ -335,6 +335,26 @@ int mfg_boxlist_destroy(mfg_boxlist* list);
  * use and when dt changes; needs a non-default stream).  Asynchronous. */
 int mfg_boxlist_step(mfg_boxlist* list, double time, double dt, int mode, void* stream);
 
+/* One coarse step of the reference's multi-level time stepping over the whole
+ * hierarchy (mflo::EvolveAMR's step, Source/mflo_evolve.cpp:26-58, and
+ * mflo::timeStep, :174-247): level l advances with dt0 / (ratio_1 ... ratio_l)
+ * (ratio_l substeps of level l per step of level l-1), each RK3 stage filling
+ * the level's ghost cells as FillPatch does (Source/mflo_gridwork.cpp:135-173):
+ * level-l data, else cell_cons_interp from level l-1 at the stage time
+ * (old / new / linear in time, mflo::GetData, Source/mflo.cpp:310-330), then
+ * the physical boundaries; the stage's face fluxes go to the flux registers
+ * (weights 1/6, 1/6, 2/3, :655-681); after the substeps of level l+1, level l
+ * is refluxed and level l+1 averaged down onto it; then the chemistry
+ * sub-steps, primitive refresh and clipping as in mfg_boxlist_step.  Needs
+ * refinement ratios 2 to 4, fine boxes aligned to the ratio and properly nested (each fine
+ * box's ghost cells and their interpolation stencil, inside the domain, lie
+ * on the next coarser level): MFG_ERR_ARG otherwise.  mode 0 plain per-box
+ * launches, 1 batched per level, 2 replay of a CUDA graph of the whole coarse
+ * step (captured on first use and when dt0 changes; non-default stream).
+ * AMReX is not vendored in the reference: the interpolation, register and
+ * average-down semantics are restated from AMReX's documented behaviour. */
+int mfg_boxlist_step_amr(mfg_boxlist* list, double time, double dt0, int mode, void* stream);
+
 /* Chooses tile size and grid size for each batched phase by timing candidates
  * (CUDA events) on this machine list, and for WENO5 the flux form (column sweep
  * or per face, bitwise equal); results (optional, 16 doubles): per phase

@@ -18,6 +18,7 @@
 // then by the physical boundary rules.  The same kernels serve the plain mode,
 // which launches per box (RHS, cut cells, bookends) and per level (fill).
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <vector>
 
@@ -46,6 +47,23 @@ struct MBox {
     int lo[3], hi[3];
     int level;
     Fab sb, sold, snew;
+    Fab cp;               // level > 0: coarse patch (coarse data around the grown box, for interpolation)
+    int cplo[3], cphi[3];
+};
+
+// Coarse data at one fill time: 0 old, 1 new, 2 a*old + b*new.
+struct TCoef {
+    int kind;
+    double a, b;
+};
+
+// One flux-register cell of a coarse-fine interface: the coarse face between
+// coarse cell cc (owned by coarse box cb, outside fine box fb) and the fine
+// box's side `side` of direction d; cf is that face in cb's face indexing,
+// ff the first of the ratio^2 fine faces in fb's.
+struct RegEnt {
+    int fb, cb, d, side;
+    int cc[3], cf[3], ff[3];
 };
 
 struct LevelG {
@@ -56,6 +74,8 @@ struct LevelG {
 };
 
 enum Phase { PH_GROWN = 0, PH_VALID, PH_FACE, PH_FLUX, PH_UPDATE, PH_COUNT };
+// per-level phases of the multi-level step: coarse-patch cells, coarsened cells of fine boxes
+enum { PH_CP = PH_COUNT, PH_AVG, PH_ALL };
 
 struct PhaseTiles {
     Tile* d = nullptr;
@@ -87,10 +107,132 @@ __device__ __forceinline__ int owner_at(const LevelG& G, const int* owner, const
     return owner[G.owner_off + m0 + (long long)G.mlen[0] * (m1 + (long long)G.mlen[1] * m2)];
 }
 
-// copy of valid data (own level, periodic images), else coarse-level injection
+__device__ __forceinline__ int floor_div(int a, int r) { return a >= 0 ? a / r : -((-a + r - 1) / r); }
+__device__ __forceinline__ double dmin_(double a, double b) { return (b < a) ? b : a; }  // std::min
+__device__ __forceinline__ double dmax_(double a, double b) { return (a < b) ? b : a; }  // std::max
+
+// cell_cons_interp (AMReX CellConservativeLinear without cross-component
+// limiting) from the coarse patch u of a box of level l (coarse level geometry
+// Gc, ratio r), for coarse cell ic and component c: MC-limited central slopes,
+// the one-sided 4-point slope at an ext_dir face of the coarse domain, and one
+// factor alpha per coarse cell keeping every fine value within the 27 coarse
+// neighbours' bounds; returns u0 and the three slopes times alpha.  A fine
+// child f of ic then gets u0 + sum_d off_d slope_d.  Explicit roundings: the
+// same operations in the same order as the CPU restatement.
+__device__ double cc_slopes(const MBox& b, const LevelG& Gc, int r, const int ic[3], int c, double sa[3]) {
+    const DevParams& P = c_P;
+    const Fab& u = b.cp;
+    const int64_t q0 = u.off(ic[0], ic[1], ic[2]) + (int64_t)c * u.ns;
+    const int64_t st[3] = {1, u.js, u.ks};
+    const double u0 = u.p[q0];
+    double sl[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double um = u.p[q0 - st[d]], up = u.p[q0 + st[d]];
+        double dc = __dmul_rn(0.5, __dsub_rn(up, um));
+        if (!Gc.per[d] && ic[d] == Gc.dlo[d] && P.bc_lo[d] == MFG_BC_EXT_DIR) {
+            if (ic[d] + 2 <= b.cphi[d])
+                dc = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(-16. / 15., um), __dmul_rn(0.5, u0)),
+                                         __dmul_rn(2. / 3., up)),
+                               __dmul_rn(0.1, u.p[q0 + 2 * st[d]]));
+            else
+                dc = __dmul_rn(0.25, __dsub_rn(__dadd_rn(up, __dmul_rn(5., u0)), __dmul_rn(6., um)));
+        }
+        if (!Gc.per[d] && ic[d] == Gc.dhi[d] && P.bc_hi[d] == MFG_BC_EXT_DIR) {
+            if (ic[d] - 2 >= b.cplo[d])
+                dc = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(16. / 15., up), __dmul_rn(0.5, u0)),
+                                         __dmul_rn(2. / 3., um)),
+                               __dmul_rn(0.1, u.p[q0 - 2 * st[d]]));
+            else
+                dc = __dmul_rn(-0.25, __dsub_rn(__dadd_rn(um, __dmul_rn(5., u0)), __dmul_rn(6., up)));
+        }
+        const double df = __dmul_rn(2.0, __dsub_rn(up, u0));
+        const double db = __dmul_rn(2.0, __dsub_rn(u0, um));
+        double sx = (__dmul_rn(df, db) >= 0.0) ? dmin_(fabs(df), fabs(db)) : 0.0;
+        sx = __dmul_rn(copysign(1.0, dc), dmin_(sx, fabs(dc)));
+        sl[d] = sx;
+    }
+    double alpha = 1.0;
+    if (sl[0] != 0.0 || sl[1] != 0.0 || sl[2] != 0.0) {
+        // (|s| (r-1)) / (2r); for r a power of two the division is the exact
+        // multiplication by 1/(2r)
+        const double f = (double)(r - 1), g = (double)(2 * r);
+        const bool pow2 = (r & (r - 1)) == 0;
+        const double ig = 1.0 / g;
+        double t[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const double x = __dmul_rn(fabs(sl[d]), f);
+            t[d] = pow2 ? __dmul_rn(x, ig) : __ddiv_rn(x, g);
+        }
+        const double dumax = __dadd_rn(__dadd_rn(t[0], t[1]), t[2]);
+        double umax = u0, umin = u0;
+        for (int kk = -1; kk <= 1; ++kk)
+            for (int jj = -1; jj <= 1; ++jj)
+#pragma unroll
+                for (int ii = -1; ii <= 1; ++ii) {
+                    const double x = u.p[q0 + ii + jj * u.js + kk * u.ks];
+                    umin = dmin_(umin, x);
+                    umax = dmax_(umax, x);
+                }
+        if (__dmul_rn(dumax, alpha) > __dsub_rn(umax, u0)) alpha = __ddiv_rn(__dsub_rn(umax, u0), dumax);
+        if (__dmul_rn(dumax, alpha) > __dsub_rn(u0, umin)) alpha = __ddiv_rn(__dsub_rn(u0, umin), dumax);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sa[d] = __dmul_rn(sl[d], alpha);
+    return u0;
+}
+
+// One coarse cell of a fine box's coarsened grown box with at least one
+// child to interpolate (a ghost cell of the box inside the periodically
+// extended fine domain that no fine box covers); bit m of mask = child
+// (m % r, (m / r) % r, m / r^2).  The hierarchy is fixed, so the list is
+// built once.
+struct IEnt {
+    int box, i, j, k;
+    unsigned long long mask;
+};
+
+// Ghost cells of the fine boxes that the fine level does not cover, by
+// cell_cons_interp: one thread per (listed coarse cell, component) computes the
+// slopes once and writes the masked children.
+__global__ void __launch_bounds__(BT) bk_cp_interp(const IEnt* __restrict__ ent, int ne,
+                                                   const MBox* __restrict__ boxes, const LevelG* __restrict__ lev) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int c = blockIdx.y;
+    const IEnt E = ent[e];
+    const MBox& b = boxes[E.box];
+    const int r = lev[b.level].ratio;
+    const int ic[3] = {E.i, E.j, E.k};
+    double sa[3];
+    const double u0 = cc_slopes(b, lev[b.level - 1], r, ic, c, sa);
+    // child offsets ((m + 0.5) / r - 0.5, m = 0..r-1; the division is exact as
+    // a multiplication for r a power of two)
+    double offs[4];
+    const bool pow2 = (r & (r - 1)) == 0;
+    for (int m = 0; m < r && m < 4; ++m) {
+        const double x = (double)m + 0.5;
+        offs[m] = __dsub_rn(pow2 ? __dmul_rn(x, 1.0 / (double)r) : __ddiv_rn(x, (double)r), 0.5);
+    }
+    unsigned long long mask = E.mask;
+    while (mask) {
+        const int m = __ffsll((long long)mask) - 1;
+        mask &= mask - 1;
+        const int mi = m % r, mj = (m / r) % r, mk = m / (r * r);
+        double v = __dadd_rn(u0, __dmul_rn(offs[mi], sa[0]));
+        v = __dadd_rn(v, __dmul_rn(offs[mj], sa[1]));
+        v = __dadd_rn(v, __dmul_rn(offs[mk], sa[2]));
+        b.sb(ic[0] * r + mi, ic[1] * r + mj, ic[2] * r + mk, c) = v;
+    }
+}
+
+// copy of valid data (own level, periodic images); where the own level has
+// none, from the coarser level: left to bk_cp_interp (interp = 1, the
+// multi-level step) or piecewise-constant injection (interp = 0)
 __global__ void __launch_bounds__(BT) bk_fill_copy(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
                                                    const int* __restrict__ owner, const Tile* __restrict__ tiles,
-                                                   int ntiles, int src, int nc) {
+                                                   int ntiles, int src, int nc, int interp) {
     TILE_LOOP
     const MBox& b = boxes[tl.box];
     int i, j, k;
@@ -110,6 +252,7 @@ __global__ void __launch_bounds__(BT) bk_fill_copy(const MBox* __restrict__ boxe
     if (!inside) continue;
     int ob = owner_at(G, owner, w);
     int cw[3] = {w[0], w[1], w[2]};
+    if (ob < 0 && b.level > 0 && interp) continue;
     if (ob < 0 && b.level > 0) {
         const LevelG& Gc = lev[b.level - 1];
         for (int d = 0; d < 3; ++d) cw[d] = Gc.dlo[d] + (w[d] - G.dlo[d]) / G.ratio;
@@ -124,14 +267,11 @@ __global__ void __launch_bounds__(BT) bk_fill_copy(const MBox* __restrict__ boxe
     TILE_END
 }
 
+// Physical boundary of one cell (i, j, k) of the array S outside the domain of
+// G in `stage` non-periodic directions (faces 1, edges 2, corners 3), from S
+// itself.
 template <int NS>
-__global__ void __launch_bounds__(BT) bk_fill_bc(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
-                                                 const Tile* __restrict__ tiles, int ntiles, int stage, int nc) {
-    TILE_LOOP
-    const MBox& b = boxes[tl.box];
-    int i, j, k;
-    grown_of(b, t, i, j, k);
-    const LevelG& G = lev[b.level];
+__device__ __forceinline__ void bc_cell(const Fab& S, const LevelG& G, int i, int j, int k, int stage, int nc) {
     const int iv[3] = {i, j, k};
     bool out[3];
     int nout = 0;
@@ -139,7 +279,7 @@ __global__ void __launch_bounds__(BT) bk_fill_bc(const MBox* __restrict__ boxes,
         out[d] = !G.per[d] && (iv[d] < G.dlo[d] || iv[d] > G.dhi[d]);
         nout += out[d];
     }
-    if (nout != stage) continue;
+    if (nout != stage) return;
     const DevParams& P = c_P;
     int dext = -1, dlast = -1;
     for (int d = 0; d < 3; ++d) {
@@ -152,7 +292,6 @@ __global__ void __launch_bounds__(BT) bk_fill_bc(const MBox* __restrict__ boxes,
     const bool lo = iv[ds] < G.dlo[ds];
     const int kind = lo ? P.bc_lo[ds] : P.bc_hi[ds];
     int sv[3] = {i, j, k};
-    const Fab& S = b.sb;
     const long long qd = S.off(i, j, k);
     if (dext >= 0) {
         sv[ds] = lo ? G.dlo[ds] : G.dhi[ds];
@@ -172,6 +311,160 @@ __global__ void __launch_bounds__(BT) bk_fill_bc(const MBox* __restrict__ boxes,
             const double x = S.p[qs + c * S.ns];
             S.p[qd + c * S.ns] = odd_at_wall(c) ? -x : x;
         }
+    }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(BT) bk_fill_bc(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
+                                                 const Tile* __restrict__ tiles, int ntiles, int stage, int nc) {
+    TILE_LOOP
+    const MBox& b = boxes[tl.box];
+    int i, j, k;
+    grown_of(b, t, i, j, k);
+    bc_cell<NS>(b.sb, lev[b.level], i, j, k, stage, nc);
+    TILE_END
+}
+
+__device__ __forceinline__ void cp_of(const MBox& b, long long t, int& i, int& j, int& k) {
+    split3(t, b.cphi[0] - b.cplo[0] + 1, b.cphi[1] - b.cplo[1] + 1, i, j, k);
+    i += b.cplo[0];
+    j += b.cplo[1];
+    k += b.cplo[2];
+}
+
+// Coarse patch of a fine box from its coarser level at one fill time (the
+// coarse half of FillPatchTwoLevels): cells inside the coarse domain (periodic
+// images included) from the owning coarse box's old / new data or their
+// linear combination; the rest by bk_cp_bc.
+__global__ void __launch_bounds__(BT) bk_cp_fill(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
+                                                 const int* __restrict__ owner, const Tile* __restrict__ tiles,
+                                                 int ntiles, const TCoef* __restrict__ coef, int ev, int nc) {
+    TILE_LOOP
+    const MBox& b = boxes[tl.box];
+    int i, j, k;
+    cp_of(b, t, i, j, k);
+    const LevelG& G = lev[b.level - 1];
+    int w[3] = {i, j, k};
+    bool inside = true;
+    for (int d = 0; d < 3; ++d) {
+        const int len = G.dhi[d] - G.dlo[d] + 1;
+        if (G.per[d]) {
+            while (w[d] < G.dlo[d]) w[d] += len;
+            while (w[d] > G.dhi[d]) w[d] -= len;
+        } else if (w[d] < G.dlo[d] || w[d] > G.dhi[d]) {
+            inside = false;
+        }
+    }
+    if (!inside) continue;
+    const int ob = owner_at(G, owner, w);
+    if (ob < 0) continue;  // excluded by the nesting check at creation
+    const MBox& o = boxes[ob];
+    const TCoef cf = coef[ev];
+    const long long q0 = o.sold.off(w[0], w[1], w[2]), q1 = o.snew.off(w[0], w[1], w[2]);
+    const long long qd = b.cp.off(i, j, k);
+    for (int c = 0; c < nc; ++c) {
+        const double x0 = o.sold.p[q0 + c * o.sold.ns], x1 = o.snew.p[q1 + c * o.snew.ns];
+        b.cp.p[qd + c * b.cp.ns] =
+            cf.kind == 0 ? x0 : cf.kind == 1 ? x1 : __dadd_rn(__dmul_rn(cf.a, x0), __dmul_rn(cf.b, x1));
+    }
+    TILE_END
+}
+
+template <int NS>
+__global__ void __launch_bounds__(BT) bk_cp_bc(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
+                                               const Tile* __restrict__ tiles, int ntiles, int stage, int nc) {
+    TILE_LOOP
+    const MBox& b = boxes[tl.box];
+    int i, j, k;
+    cp_of(b, t, i, j, k);
+    bc_cell<NS>(b.cp, lev[b.level - 1], i, j, k, stage, nc);
+    TILE_END
+}
+
+// Flux registers (AMReX FluxRegister).  One thread per (register cell, advected
+// component c); registers are stored component-major, reg[c * ne + e].
+// CrseInit(ADD): reg += F_coarse * scale_d
+__global__ void __launch_bounds__(BT) bk_reg_crse(const RegEnt* __restrict__ ent, int ne,
+                                                  const RhsBox* __restrict__ rhs, double* __restrict__ reg,
+                                                  double s0, double s1, double s2) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int c = blockIdx.y;
+    const RegEnt E = ent[e];
+    const Fab& F = rhs[E.cb].flx[E.d];
+    const double scale = E.d == 0 ? s0 : E.d == 1 ? s1 : s2;
+    double& r = reg[(size_t)c * ne + e];
+    r = __dadd_rn(r, __dmul_rn(F.p[F.off(E.cf[0], E.cf[1], E.cf[2]) + c * F.ns], scale));
+}
+
+// FineAdd: reg += scale_d * F_fine over the ratio^2 fine faces, the higher
+// transverse direction outer
+__global__ void __launch_bounds__(BT) bk_reg_fine(const RegEnt* __restrict__ ent, int ne,
+                                                  const RhsBox* __restrict__ rhs, double* __restrict__ reg,
+                                                  double s0, double s1, double s2, int ratio) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int c = blockIdx.y;
+    const RegEnt E = ent[e];
+    const Fab& F = rhs[E.fb].flx[E.d];
+    const double scale = E.d == 0 ? s0 : E.d == 1 ? s1 : s2;
+    const int t1 = E.d == 0 ? 1 : 0, t2 = E.d == 2 ? 1 : 2;
+    const int64_t st[3] = {1, F.js, F.ks};
+    const int64_t q = F.off(E.ff[0], E.ff[1], E.ff[2]) + c * F.ns;
+    double v = reg[(size_t)c * ne + e];
+    for (int o2 = 0; o2 < ratio; ++o2)
+        for (int o1 = 0; o1 < ratio; ++o1) v = __dadd_rn(v, __dmul_rn(scale, F.p[q + o1 * st[t1] + o2 * st[t2]]));
+    reg[(size_t)c * ne + e] = v;
+}
+
+// Reflux of one orientation (entries e0..e1): the coarse cell outside the fine
+// box gets -reg/vol (low side) or +reg/vol (high side), every state component
+// (zero register for the non-advected ones).
+__global__ void __launch_bounds__(BT) bk_reflux(const RegEnt* __restrict__ ent, int e0, int e1, int ne,
+                                                const MBox* __restrict__ boxes, const double* __restrict__ reg,
+                                                double vol) {
+    const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= e1) return;
+    const int n = blockIdx.y;
+    const RegEnt E = ent[e];
+    int c = -1;
+    if (n < NCONS) c = n;
+    else if (n >= NFLO) c = n - (NFLO - NCONS);
+    const double f = c >= 0 ? reg[(size_t)c * ne + e] : 0.0;
+    double& x = boxes[E.cb].snew(E.cc[0], E.cc[1], E.cc[2], n);
+    x = __dadd_rn(x, E.side ? __ddiv_rn(f, vol) : __ddiv_rn(-f, vol));
+}
+
+__device__ __forceinline__ void avg_of(const MBox& b, int r, long long t, int& i, int& j, int& k) {
+    const int a0 = floor_div(b.lo[0], r), a1 = floor_div(b.lo[1], r), a2 = floor_div(b.lo[2], r);
+    split3(t, floor_div(b.hi[0] + 1, r) - a0, floor_div(b.hi[1] + 1, r) - a1, i, j, k);
+    i += a0;
+    j += a1;
+    k += a2;
+}
+
+// average_down of a fine box onto the coarse cells it covers, every component:
+// crse = (1/r^3) * sum of the fine cells (k, j, i order, from 0)
+__global__ void __launch_bounds__(BT) bk_avgdown(const MBox* __restrict__ boxes, const LevelG* __restrict__ lev,
+                                                 const int* __restrict__ owner, const Tile* __restrict__ tiles,
+                                                 int ntiles, int nc) {
+    TILE_LOOP
+    const MBox& b = boxes[tl.box];
+    const int r = lev[b.level].ratio;
+    int i, j, k;
+    avg_of(b, r, t, i, j, k);
+    const int w[3] = {i, j, k};
+    const int ob = owner_at(lev[b.level - 1], owner, w);
+    if (ob < 0) continue;
+    const Fab& C = boxes[ob].snew;
+    const Fab& F = b.snew;
+    const double volfrac = 1.0 / (double)(r * r * r);
+    for (int n = 0; n < nc; ++n) {
+        double acc = 0.0;
+        for (int kr = 0; kr < r; ++kr)
+            for (int jr = 0; jr < r; ++jr)
+                for (int ir = 0; ir < r; ++ir) acc = __dadd_rn(acc, F(i * r + ir, j * r + jr, k * r + kr, n));
+        C(i, j, k, n) = __dmul_rn(volfrac, acc);
     }
     TILE_END
 }
@@ -342,6 +635,25 @@ struct mfg_boxlist {
     cudaGraphExec_t gexec = nullptr;
     double gdt = 0.0;
     long long cells = 0;
+    // multi-level step (mfg_boxlist_step_amr)
+    int amr_rc = MFG_ERR_STATE;            // MFG_OK when the hierarchy is aligned and properly nested
+    double* d_cp = nullptr;                // coarse patches of the boxes of levels > 0
+    std::vector<PhaseTiles> lt;            // per level and phase (level * PH_ALL + phase)
+    int lt_version = -1;                   // tile_version the per-level lists were built for
+    int tile_version = 0;                  // bumped whenever the all-box tile lists change
+    std::vector<RegEnt*> d_ent;            // [l]: register cells of the l / l-1 interface
+    std::vector<IEnt*> d_ient;             // [l]: coarse cells with fine ghost children to interpolate
+    std::vector<int> nient;
+    std::vector<double*> d_reg;
+    std::vector<int> nent;
+    std::vector<std::array<int, 7>> eoff;  // [l]: first entry of each orientation (x-lo, y-lo, z-lo, x-hi, ...)
+    TCoef* d_coef = nullptr;
+    std::vector<TCoef> hcoef;
+    int nevents = 0;
+    cudaGraphExec_t gexec_amr = nullptr;
+    double gdt_amr = 0.0;
+    int lt_flux_kind = -1;
+    std::vector<int> h_owner;              // host copy of the owner maps
 };
 
 namespace {
@@ -368,6 +680,16 @@ long long items_of(const mfg_boxlist& L, int ph, int b, int part) {
             const int d = part >> 5;
             if (flux_kind(L) == 2) return sweep_items(L.rhs[b], d);
             return (n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2));
+        }
+        case PH_CP: {
+            if (x.level == 0) return 0;
+            const MBox& m = L.mbox[b];
+            return (long long)(m.cphi[0] - m.cplo[0] + 1) * (m.cphi[1] - m.cplo[1] + 1) * (m.cphi[2] - m.cplo[2] + 1);
+        }
+        case PH_AVG: {
+            if (x.level == 0) return 0;
+            const long long r = L.levg[x.level].ratio;
+            return (n[0] / r) * (n[1] / r) * (n[2] / r);
         }
     }
     return 0;
@@ -399,7 +721,8 @@ cudaError_t build_tiles(mfg_boxlist& L, PhaseTiles& P, int ph, int tile_items, i
         }
     }
     free_tiles(P);
-    if (ph == PH_FLUX) L.flux_tiles_kind = flux_kind(L);
+    if (ph == PH_FLUX && level < 0) L.flux_tiles_kind = flux_kind(L);
+    if (level < 0) ++L.tile_version;
     P.tile_items = tile_items;
     P.n = (int)t.size();
     P.grid = P.grid_cap > 0 ? std::min(P.n, P.grid_cap) : P.n;
@@ -423,12 +746,28 @@ int ns_bucket(int ns) { return ns <= 1 ? 1 : ns <= 2 ? 2 : ns <= 4 ? 4 : ns <= 8
     }
 
 // ---- batched phases --------------------------------------------------------------
-void b_fill(mfg_boxlist& L, const PhaseTiles& T, int src, cudaStream_t st) {
+// The tile lists a phase runs over: every box, or the boxes of one level.
+struct TSet {
+    const PhaseTiles* t[PH_ALL];
+    const PhaseTiles& operator[](int p) const { return *t[p]; }
+};
+TSet all_tiles(const mfg_boxlist& L) {
+    TSet s;
+    for (int p = 0; p < PH_ALL; ++p) s.t[p] = p < PH_COUNT ? &L.ph[p] : nullptr;
+    return s;
+}
+TSet level_tiles(const mfg_boxlist& L, int l) {
+    TSet s;
+    for (int p = 0; p < PH_ALL; ++p) s.t[p] = &L.lt[(size_t)l * PH_ALL + p];
+    return s;
+}
+
+void b_fill(mfg_boxlist& L, const PhaseTiles& T, int src, cudaStream_t st, int interp = 0) {
     if (!T.n) return;
     const int nc = NFLO + c_host_params().nspec;
     {
         ProfScope ps(K_FILL_COPY, st);
-        bk_fill_copy<<<T.grid, BT, 0, st>>>(L.d_mbox, L.d_lev, L.d_owner, T.d, T.n, src, nc);
+        bk_fill_copy<<<T.grid, BT, 0, st>>>(L.d_mbox, L.d_lev, L.d_owner, T.d, T.n, src, nc, interp);
     }
     for (int s = 1; s <= 3; ++s) {
         ProfScope ps(K_FILL_BC, st);
@@ -436,28 +775,27 @@ void b_fill(mfg_boxlist& L, const PhaseTiles& T, int src, cudaStream_t st) {
     }
 }
 
-void b_cutcells(mfg_boxlist& L, cudaStream_t st) {
-    const PhaseTiles& T = L.ph[PH_VALID];
+void b_cutcells(mfg_boxlist& L, const PhaseTiles& T, cudaStream_t st) {
     ProfScope ps(K_CUT, st);
     cudaMemsetAsync(L.d_count, 0, sizeof(unsigned), st);
     bk_cut_list<<<T.grid, BT, 0, st>>>(L.d_cut, T.d, T.n, L.d_cutlist, L.d_count);
     NS_DISPATCH(bk_cut, (L.cut_grid, BT, 0, st), (L.d_cut, L.d_cutlist, L.d_count));
 }
 
-void b_rhs(mfg_boxlist& L, int stage, double dt, cudaStream_t st) {
+void b_rhs(mfg_boxlist& L, const TSet& TS, int stage, double dt, cudaStream_t st) {
     const int ord = c_host_params().order_hyp;
     if (ord >= 4) {
-        const PhaseTiles& T = L.ph[PH_GROWN];
+        const PhaseTiles& T = TS[PH_GROWN];
         ProfScope ps(K_PRIM, st);
         NS_DISPATCH(bk_prim, (T.grid, BT, 0, st), (L.d_rhs, T.d, T.n));
     }
     {
-        const PhaseTiles& T = L.ph[PH_FACE];
+        const PhaseTiles& T = TS[PH_FACE];
         ProfScope ps(K_FACE, st);
         NS_DISPATCH(bk_face, (T.grid, BT, 0, st), (L.d_rhs, T.d, T.n));
     }
     if (!(c_host_params().do_ns && ord <= 2)) {
-        const PhaseTiles& T = L.ph[PH_FLUX];
+        const PhaseTiles& T = TS[PH_FLUX];
         ProfScope ps(K_FLUX, st);
         if (flux_kind(L) == 2)
             bk_flux_sweep<<<T.grid, SWEEP_BT, 0, st>>>(L.d_rhs, T.d, T.n);
@@ -469,7 +807,7 @@ void b_rhs(mfg_boxlist& L, int stage, double dt, cudaStream_t st) {
             bk_flux<false><<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n);
     }
     {
-        const PhaseTiles& T = L.ph[PH_UPDATE];
+        const PhaseTiles& T = TS[PH_UPDATE];
         ProfScope ps(K_UPDATE, st);
         bk_update<<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n, stage, dt);
     }
@@ -482,10 +820,11 @@ void step_batched(mfg_boxlist& L, double dt, cudaStream_t st) {
         ProfScope ps(K_COPY, st);
         bk_copy_old<<<V.grid, BT, 0, st>>>(L.d_mbox, V.d, V.n, nc);
     }
+    const TSet T = all_tiles(L);
     for (int stage = 1; stage <= 3; ++stage) {
         b_fill(L, L.ph[PH_GROWN], stage == 1 ? 0 : 1, st);
-        b_cutcells(L, st);
-        b_rhs(L, stage, dt, st);
+        b_cutcells(L, L.ph[PH_VALID], st);
+        b_rhs(L, T, stage, dt, st);
     }
     {
         ProfScope ps(K_COPY, st);
@@ -534,6 +873,417 @@ int step_plain(mfg_boxlist& L, double dt, cudaStream_t st) {
 void drop_graph(mfg_boxlist& L) {
     if (L.gexec) cudaGraphExecDestroy(L.gexec);
     L.gexec = nullptr;
+    if (L.gexec_amr) cudaGraphExecDestroy(L.gexec_amr);
+    L.gexec_amr = nullptr;
+}
+
+// ---- multi-level step -------------------------------------------------------------
+// mflo::timeStep (Source/mflo_evolve.cpp:174-247) over the whole hierarchy:
+// level l advances with dt_l = dt_{l-1} / ratio_l (ratio_l substeps per step
+// of level l-1).  Each stage fills the level's ghost cells (FillPatch,
+// Source/mflo_gridwork.cpp:135-173: for l > 0 the coarse patch of each box
+// from level l-1 at the stage time, its physical boundaries, then
+// cell_cons_interp where level l has no data), runs cut cells and the RHS
+// with the stage update, and adds the stage's face fluxes to the flux
+// registers (CrseInit on the finer interface with -dt dA w, FineAdd on the
+// coarser one with dt dA w; w = 1/6, 1/6, 2/3, Source/mflo_evolve.cpp:
+// 655-681); then the chemistry sub-step.  After the substeps of level l+1,
+// level l is refluxed and level l+1 averaged down onto it; after the coarse
+// step, primitive refresh and clipping of every box.
+constexpr double kTwo3rd = 0.6666666666666666667;  // Source/mflo_constants.H two3rd, sixth
+constexpr double kSixth = kTwo3rd * 0.5 * 0.5;
+
+int hfloor_div(int a, int r) { return a >= 0 ? a / r : -((-a + r - 1) / r); }
+
+bool hwrap(const LevelG& G, const int iv[3], int w[3]) {
+    bool inside = true;
+    for (int d = 0; d < 3; ++d) {
+        const int len = G.dhi[d] - G.dlo[d] + 1;
+        w[d] = iv[d];
+        if (G.per[d]) {
+            while (w[d] < G.dlo[d]) w[d] += len;
+            while (w[d] > G.dhi[d]) w[d] -= len;
+        } else if (w[d] < G.dlo[d] || w[d] > G.dhi[d]) {
+            inside = false;
+        }
+    }
+    return inside;
+}
+
+int howner(const mfg_boxlist& L, int l, const int w[3]) {
+    const LevelG& G = L.levg[l];
+    const int m0 = (w[0] - G.dlo[0]) / G.gran, m1 = (w[1] - G.dlo[1]) / G.gran, m2 = (w[2] - G.dlo[2]) / G.gran;
+    return L.h_owner[G.owner_off + m0 + (long long)G.mlen[0] * (m1 + (long long)G.mlen[1] * m2)];
+}
+
+// Coarse patches, nesting and alignment checks, flux registers.  A hierarchy
+// that fails a check keeps amr_rc = MFG_ERR_ARG (the common-dt step still works).
+cudaError_t setup_amr(mfg_boxlist& L) {
+    const int nlev = L.nlev, nc = NFLO + c_host_params().nspec, C = NCONS + c_host_params().nspec;
+    int rc = MFG_OK;
+    for (int l = 1; l < nlev; ++l) {
+        const int r = L.levg[l].ratio;
+        const mfg_geom &gc = L.geoms[l - 1], &gf = L.geoms[l];
+        if (r < 2 || r > 4) rc = MFG_ERR_ARG;  // refinement ratios 2, 3, 4
+        for (int d = 0; d < 3 && !rc; ++d) {
+            if (gf.domain_lo[d] != gc.domain_lo[d] * r || gf.domain_hi[d] + 1 != (gc.domain_hi[d] + 1) * r ||
+                gf.is_periodic[d] != gc.is_periodic[d] || std::fabs(gc.dx[d] / gf.dx[d] - r) > 1e-9 * r)
+                rc = MFG_ERR_ARG;
+        }
+    }
+    // coarse patches
+    size_t tot = 0;
+    std::vector<size_t> off(L.nbox, 0);
+    for (int b = 0; b < L.nbox && !rc; ++b) {
+        MBox& m = L.mbox[b];
+        if (m.level == 0) continue;
+        const int r = L.levg[m.level].ratio;
+        size_t n = 1;
+        for (int d = 0; d < 3; ++d) {
+            if (hfloor_div(m.lo[d], r) * r != m.lo[d] || hfloor_div(m.hi[d] + 1, r) * r != m.hi[d] + 1) rc = MFG_ERR_ARG;
+            m.cplo[d] = hfloor_div(m.lo[d] - MFG_NGROW, r) - 1;
+            m.cphi[d] = hfloor_div(m.hi[d] + MFG_NGROW, r) + 1;
+            n *= (size_t)(m.cphi[d] - m.cplo[d] + 1);
+            // a reflecting boundary mirrors the patch's outside layers onto its inside ones
+            const LevelG& G = L.levg[m.level - 1];
+            if (!G.per[d]) {
+                const int inside = std::min(m.cphi[d], G.dhi[d]) - std::max(m.cplo[d], G.dlo[d]) + 1;
+                if (inside < std::max(G.dlo[d] - m.cplo[d], m.cphi[d] - G.dhi[d])) rc = MFG_ERR_ARG;
+            }
+        }
+        off[b] = tot;
+        tot += n;
+    }
+    // nesting: every coarse-patch cell inside the coarse domain lies on the coarse level
+    for (int b = 0; b < L.nbox && !rc; ++b) {
+        const MBox& m = L.mbox[b];
+        if (m.level == 0) continue;
+        for (int k = m.cplo[2]; k <= m.cphi[2] && !rc; ++k)
+            for (int j = m.cplo[1]; j <= m.cphi[1] && !rc; ++j)
+                for (int i = m.cplo[0]; i <= m.cphi[0] && !rc; ++i) {
+                    const int iv[3] = {i, j, k};
+                    int w[3];
+                    if (hwrap(L.levg[m.level - 1], iv, w) && howner(L, m.level - 1, w) < 0) rc = MFG_ERR_ARG;
+                }
+    }
+    // coarse cells with fine ghost children to interpolate, per level
+    std::vector<std::vector<IEnt>> ients(nlev);
+    for (int b = 0; b < L.nbox && !rc; ++b) {
+        const MBox& m = L.mbox[b];
+        if (m.level == 0) continue;
+        const int l = m.level, r = L.levg[l].ratio;
+        const LevelG& G = L.levg[l];
+        for (int k = m.cplo[2] + 1; k < m.cphi[2]; ++k)
+            for (int j = m.cplo[1] + 1; j < m.cphi[1]; ++j)
+                for (int i = m.cplo[0] + 1; i < m.cphi[0]; ++i) {
+                    unsigned long long mask = 0;
+                    for (int mk = 0; mk < r; ++mk)
+                        for (int mj = 0; mj < r; ++mj)
+                            for (int mi = 0; mi < r; ++mi) {
+                                const int fv[3] = {i * r + mi, j * r + mj, k * r + mk};
+                                bool ghost = false, grown = true;
+                                for (int d = 0; d < 3; ++d) {
+                                    ghost |= fv[d] < m.lo[d] || fv[d] > m.hi[d];
+                                    grown &= fv[d] >= m.lo[d] - MFG_NGROW && fv[d] <= m.hi[d] + MFG_NGROW;
+                                }
+                                int w[3];
+                                if (!ghost || !grown || !hwrap(G, fv, w) || howner(L, l, w) >= 0) continue;
+                                mask |= 1ull << (mi + r * (mj + r * mk));
+                            }
+                    if (mask) ients[l].push_back(IEnt{b, i, j, k, mask});
+                }
+    }
+    // flux registers, in the order x-lo, y-lo, z-lo, x-hi, y-hi, z-hi
+    L.d_ent.assign(nlev, nullptr);
+    L.d_reg.assign(nlev, nullptr);
+    L.nent.assign(nlev, 0);
+    L.eoff.assign(nlev, std::array<int, 7>{});
+    std::vector<std::vector<RegEnt>> ents(nlev);
+    for (int l = 1; l < nlev && !rc; ++l) {
+        const int r = L.levg[l].ratio;
+        for (int side = 0; side < 2; ++side)
+            for (int d = 0; d < 3; ++d) {
+                L.eoff[l][d + 3 * side] = (int)ents[l].size();
+                for (int fb = 0; fb < L.nbox && !rc; ++fb) {
+                    const MBox& m = L.mbox[fb];
+                    if (m.level != l) continue;
+                    const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+                    const int fface = side ? m.hi[d] + 1 : m.lo[d];
+                    const int cface = hfloor_div(fface, r);
+                    for (int q2 = hfloor_div(m.lo[t2], r); q2 <= hfloor_div(m.hi[t2] + 1, r) - 1; ++q2)
+                        for (int q1 = hfloor_div(m.lo[t1], r); q1 <= hfloor_div(m.hi[t1] + 1, r) - 1; ++q1) {
+                            int cc[3];
+                            cc[d] = side ? cface : cface - 1;
+                            cc[t1] = q1;
+                            cc[t2] = q2;
+                            int w[3];
+                            if (!hwrap(L.levg[l - 1], cc, w)) continue;
+                            const int fw[3] = {w[0] * r, w[1] * r, w[2] * r};
+                            if (howner(L, l, fw) >= 0) continue;  // covered: average_down overwrites it
+                            const int cb = howner(L, l - 1, w);
+                            if (cb < 0) {
+                                rc = MFG_ERR_ARG;
+                                break;
+                            }
+                            RegEnt e;
+                            e.fb = fb;
+                            e.cb = cb;
+                            e.d = d;
+                            e.side = side;
+                            for (int q = 0; q < 3; ++q) e.cc[q] = e.cf[q] = w[q];
+                            e.cf[d] = side ? w[d] : w[d] + 1;
+                            e.ff[d] = fface;
+                            e.ff[t1] = q1 * r;
+                            e.ff[t2] = q2 * r;
+                            ents[l].push_back(e);
+                        }
+                }
+            }
+        L.eoff[l][6] = (int)ents[l].size();
+    }
+    L.amr_rc = rc;
+    if (rc) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaMalloc(&L.d_cp, std::max<size_t>(tot * nc, 1) * sizeof(double))) != cudaSuccess) return e;
+    cudaMemsetAsync(L.d_cp, 0, std::max<size_t>(tot * nc, 1) * sizeof(double));
+    for (int b = 0; b < L.nbox; ++b) {
+        MBox& m = L.mbox[b];
+        if (m.level == 0) continue;
+        int len[3];
+        for (int d = 0; d < 3; ++d) len[d] = m.cphi[d] - m.cplo[d] + 1;
+        m.cp = dense_fab(L.d_cp + off[b] * nc, m.cplo, len);
+    }
+    if ((e = cudaMemcpy(L.d_mbox, L.mbox.data(), L.nbox * sizeof(MBox), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
+    L.d_ient.assign(nlev, nullptr);
+    L.nient.assign(nlev, 0);
+    for (int l = 1; l < nlev; ++l) {
+        const size_t ni = ients[l].size();
+        L.nient[l] = (int)ni;
+        if ((e = cudaMalloc(&L.d_ient[l], std::max<size_t>(ni, 1) * sizeof(IEnt))) != cudaSuccess) return e;
+        if (ni && (e = cudaMemcpy(L.d_ient[l], ients[l].data(), ni * sizeof(IEnt), cudaMemcpyHostToDevice)) !=
+                      cudaSuccess)
+            return e;
+    }
+    for (int l = 1; l < nlev; ++l) {
+        const size_t ne = ents[l].size();
+        L.nent[l] = (int)ne;
+        if ((e = cudaMalloc(&L.d_ent[l], std::max<size_t>(ne, 1) * sizeof(RegEnt))) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&L.d_reg[l], std::max<size_t>(ne * C, 1) * sizeof(double))) != cudaSuccess) return e;
+        if (ne && (e = cudaMemcpy(L.d_ent[l], ents[l].data(), ne * sizeof(RegEnt), cudaMemcpyHostToDevice)) !=
+                      cudaSuccess)
+            return e;
+    }
+    int nev = 0, sub = 1;
+    for (int l = 1; l < nlev; ++l) {
+        sub *= L.levg[l].ratio;
+        nev += 3 * sub;
+    }
+    L.nevents = nev;
+    L.hcoef.assign(std::max(nev, 1), TCoef{0, 0.0, 0.0});
+    return cudaMalloc(&L.d_coef, std::max(nev, 1) * sizeof(TCoef));
+}
+
+// Per-level tile lists with the settings of the all-box lists.
+cudaError_t build_level_tiles(mfg_boxlist& L) {
+    L.lt.resize((size_t)L.nlev * PH_ALL);
+    for (int l = 0; l < L.nlev; ++l)
+        for (int p = 0; p < PH_ALL; ++p) {
+            const PhaseTiles& src = L.ph[p < PH_COUNT ? p : PH_GROWN];
+            PhaseTiles& P = L.lt[(size_t)l * PH_ALL + p];
+            P.grid_cap = src.grid_cap;
+            cudaError_t e = build_tiles(L, P, p, src.tile_items, l);
+            if (e != cudaSuccess) return e;
+        }
+    L.lt_version = L.tile_version;
+    L.lt_flux_kind = flux_kind(L);
+    return cudaSuccess;
+}
+
+struct AmrRun {
+    std::vector<double> t_old, t_new, dt;
+    int ev = 0;
+    bool launch = false;
+    int mode = 1;
+    cudaStream_t st = nullptr;
+    int rc = MFG_OK;
+};
+
+// Coarse data of level l at time T (mflo::GetData, Source/mflo.cpp:310-330):
+// new / old within 1e-3 dt of t_new / t_old, else their linear combination.
+int amr_coef(mfg_boxlist& L, AmrRun& R, int l, double T) {
+    TCoef c{0, 0.0, 0.0};
+    const double teps = (R.t_new[l] - R.t_old[l]) * 1.e-3;
+    if (T > R.t_new[l] - teps && T < R.t_new[l] + teps) {
+        c.kind = 1;
+    } else if (T > R.t_old[l] - teps && T < R.t_old[l] + teps) {
+        c.kind = 0;
+    } else {
+        const double t0 = R.t_old[l], t1 = R.t_new[l];
+        c.kind = 2;
+        c.a = (t1 - T) / (t1 - t0);
+        c.b = (T - t0) / (t1 - t0);
+    }
+    L.hcoef[R.ev] = c;
+    return R.ev++;
+}
+
+void amr_note(AmrRun& R, cudaError_t e) {
+    if (e != cudaSuccess && R.rc == MFG_OK) R.rc = MFG_ERR_CUDA;
+}
+
+void amr_fill(mfg_boxlist& L, AmrRun& R, int l, int src, int ev) {
+    const TSet T = level_tiles(L, l);
+    const int nc = NFLO + c_host_params().nspec;
+    cudaStream_t st = R.st;
+    if (l > 0 && T[PH_CP].n) {
+        const PhaseTiles& C = T[PH_CP];
+        {
+            ProfScope ps(K_AMR_PATCH, st);
+            bk_cp_fill<<<C.grid, BT, 0, st>>>(L.d_mbox, L.d_lev, L.d_owner, C.d, C.n, L.d_coef, ev, nc);
+        }
+        for (int s = 1; s <= 3; ++s) {
+            ProfScope ps(K_AMR_PATCH, st);
+            NS_DISPATCH(bk_cp_bc, (C.grid, BT, 0, st), (L.d_mbox, L.d_lev, C.d, C.n, s, nc));
+        }
+        const int ni = L.nient[l];
+        ProfScope ps(K_AMR_INTERP, st);
+        if (ni) bk_cp_interp<<<dim3((ni + BT - 1) / BT, nc), BT, 0, st>>>(L.d_ient[l], ni, L.d_mbox, L.d_lev);
+    }
+    b_fill(L, T[PH_GROWN], src, st, 1);
+}
+
+void amr_copy_old(mfg_boxlist& L, AmrRun& R, int l) {
+    const int nc = NFLO + c_host_params().nspec;
+    if (R.mode == 0) {
+        Fab none;
+        memset(&none, 0, sizeof(none));
+        for (int b = 0; b < L.nbox; ++b)
+            if (L.boxes[b].level == l)
+                amr_note(R, launch_axpy_valid(L.boxes[b], make_fab(L.boxes[b].s_old), none, 0.0, true,
+                                              make_fab(L.boxes[b].s_new), nc, R.st));
+        return;
+    }
+    const PhaseTiles& V = level_tiles(L, l)[PH_VALID];
+    if (!V.n) return;
+    ProfScope ps(K_COPY, R.st);
+    bk_copy_old<<<V.grid, BT, 0, R.st>>>(L.d_mbox, V.d, V.n, nc);
+}
+
+void amr_stage(mfg_boxlist& L, AmrRun& R, int l, int stage, double dtl) {
+    cudaStream_t st = R.st;
+    if (R.mode == 0) {
+        for (int b = 0; b < L.nbox; ++b)
+            if (L.boxes[b].level == l)
+                amr_note(R, launch_cutcells_box(L.boxes[b], L.geoms[l], nullptr, L.d_plainlist, L.d_count + 1, st));
+        for (int b = 0; b < L.nbox; ++b)
+            if (L.boxes[b].level == l) amr_note(R, launch_rhs_box(L.rhs[b], stage, dtl, weno_fast_mode(), st));
+    } else {
+        const TSet T = level_tiles(L, l);
+        if (T[PH_VALID].n) {
+            b_cutcells(L, T[PH_VALID], st);
+            b_rhs(L, T, stage, dtl, st);
+        }
+    }
+    // flux registers
+    const int C = NCONS + c_host_params().nspec;
+    const double ff = stage < 3 ? kSixth : kTwo3rd;
+    const double* dx = L.geoms[l].dx;
+    const double dA[3] = {dx[1] * dx[2], dx[0] * dx[2], dx[0] * dx[1]};
+    ProfScope ps(K_AMR_SYNC, st);
+    if (l + 1 < L.nlev && L.nent[l + 1]) {
+        const int ne = L.nent[l + 1];
+        bk_reg_crse<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l + 1], ne, L.d_rhs, L.d_reg[l + 1],
+                                                               -dtl * dA[0] * ff, -dtl * dA[1] * ff, -dtl * dA[2] * ff);
+    }
+    if (l > 0 && L.nent[l]) {
+        const int ne = L.nent[l];
+        bk_reg_fine<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l], ne, L.d_rhs, L.d_reg[l], dtl * dA[0] * ff,
+                                                               dtl * dA[1] * ff, dtl * dA[2] * ff, L.levg[l].ratio);
+    }
+}
+
+void amr_chem(mfg_boxlist& L, AmrRun& R, int l, double dtl) {
+    const int nc = NFLO + c_host_params().nspec;
+    if (R.mode == 0) {
+        for (int b = 0; b < L.nbox; ++b)
+            if (L.boxes[b].level == l) amr_note(R, launch_chem_substep(L.boxes[b], dtl, R.st));
+        return;
+    }
+    const PhaseTiles& V = level_tiles(L, l)[PH_VALID];
+    if (!V.n) return;
+    ProfScope ps(K_CHEM, R.st);
+    NS_DISPATCH(bk_chem, (V.grid, BT, 0, R.st), (L.d_mbox, V.d, V.n, dtl, nc));
+}
+
+void amr_sync(mfg_boxlist& L, AmrRun& R, int l) {  // reflux of level l, average_down of l+1 onto l
+    cudaStream_t st = R.st;
+    const int nc = NFLO + c_host_params().nspec;
+    ProfScope ps(K_AMR_SYNC, st);
+    const double* dx = L.geoms[l].dx;
+    const double vol = dx[0] * dx[1] * dx[2];
+    const int ne = L.nent[l + 1];
+    for (int o = 0; o < 6; ++o) {
+        const int e0 = L.eoff[l + 1][o], e1 = L.eoff[l + 1][o + 1];
+        if (e1 > e0)
+            bk_reflux<<<dim3((e1 - e0 + BT - 1) / BT, nc), BT, 0, st>>>(L.d_ent[l + 1], e0, e1, ne, L.d_mbox,
+                                                                      L.d_reg[l + 1], vol);
+    }
+    const PhaseTiles& A = level_tiles(L, l + 1)[PH_AVG];
+    if (A.n) bk_avgdown<<<A.grid, BT, 0, st>>>(L.d_mbox, L.d_lev, L.d_owner, A.d, A.n, nc);
+}
+
+void amr_advance(mfg_boxlist& L, AmrRun& R, int l, double time, double dtl) {
+    if (R.launch) amr_copy_old(L, R, l);
+    R.t_old[l] = R.t_new[l];
+    R.t_new[l] += dtl;
+    if (R.launch && l + 1 < L.nlev && L.nent[l + 1])
+        amr_note(R, cudaMemsetAsync(L.d_reg[l + 1], 0,
+                                    (size_t)L.nent[l + 1] * (NCONS + c_host_params().nspec) * sizeof(double), R.st));
+    for (int stage = 1; stage <= 3; ++stage) {
+        const double T = stage == 1 ? time : time + dtl;
+        const int ev = l > 0 ? amr_coef(L, R, l - 1, T) : -1;
+        if (!R.launch) continue;
+        amr_fill(L, R, l, stage == 1 ? 0 : 1, ev);
+        amr_stage(L, R, l, stage, dtl);
+    }
+    if (R.launch) {
+        amr_copy_old(L, R, l);
+        amr_chem(L, R, l, dtl);
+    }
+}
+
+void amr_time_step(mfg_boxlist& L, AmrRun& R, int l, double time) {
+    amr_advance(L, R, l, time, R.dt[l]);
+    if (l + 1 < L.nlev) {
+        for (int i = 1; i <= L.levg[l + 1].ratio; ++i) amr_time_step(L, R, l + 1, time + (i - 1) * R.dt[l + 1]);
+        if (R.launch) amr_sync(L, R, l);
+    }
+}
+
+int amr_run(mfg_boxlist& L, double time, double dt0, bool launch, int mode, cudaStream_t st) {
+    AmrRun R;
+    R.launch = launch;
+    R.mode = mode;
+    R.st = st;
+    R.t_old.assign(L.nlev, time);
+    R.t_new.assign(L.nlev, time);
+    R.dt.assign(L.nlev, dt0);
+    for (int l = 1; l < L.nlev; ++l) R.dt[l] = R.dt[l - 1] / L.levg[l].ratio;
+    amr_time_step(L, R, 0, time);
+    if (!launch) return MFG_OK;
+    if (mode == 0) {
+        for (int b = 0; b < L.nbox; ++b) {
+            amr_note(R, launch_update_prims(L.boxes[b], nullptr, st));
+            amr_note(R, launch_clip_species(L.boxes[b], st));
+        }
+    } else {
+        const PhaseTiles& V = L.ph[PH_VALID];
+        ProfScope ps(K_PRIMS, st);
+        NS_DISPATCH(bk_prims, (V.grid, BT, 0, st), (L.d_mbox, V.d, V.n, c_host_params().nspec, 1));
+    }
+    amr_note(R, cudaGetLastError());
+    return R.rc;
 }
 
 int sm_count() {
@@ -655,6 +1405,7 @@ int mfg_boxlist_create(const mfg_box* boxes, int nbox, const mfg_geom* geoms, in
         if ((e = cudaMalloc(&L->d_owner, std::max<size_t>(own.size(), 1) * sizeof(int))) != cudaSuccess) goto fail;
         if ((e = cudaMemcpy(L->d_owner, own.data(), own.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
             goto fail;
+        L->h_owner.swap(own);
     }
     if ((e = cudaMalloc(&L->d_rhs, nbox * sizeof(RhsBox))) != cudaSuccess) goto fail;
     if ((e = cudaMalloc(&L->d_cut, nbox * sizeof(CutBox))) != cudaSuccess) goto fail;
@@ -684,6 +1435,7 @@ int mfg_boxlist_create(const mfg_box* boxes, int nbox, const mfg_geom* geoms, in
                 }
         if ((e = cudaMemcpyToSymbol(c_wdir, w, sizeof(w))) != cudaSuccess) goto fail;
     }
+    if ((e = setup_amr(*L)) != cudaSuccess) goto fail;
     *out = L;
     return MFG_OK;
 fail:
@@ -696,6 +1448,12 @@ int mfg_boxlist_destroy(mfg_boxlist* L) {
     drop_graph(*L);
     for (int p = 0; p < PH_COUNT; ++p) free_tiles(L->ph[p]);
     for (auto& t : L->level_grown) free_tiles(t);
+    for (auto& t : L->lt) free_tiles(t);
+    for (double* r : L->d_reg) cudaFree(r);
+    for (IEnt* r : L->d_ient) cudaFree(r);
+    for (RegEnt* r : L->d_ent) cudaFree(r);
+    cudaFree(L->d_cp);
+    cudaFree(L->d_coef);
     cudaFree(L->d_rhs);
     cudaFree(L->d_cut);
     cudaFree(L->d_mbox);
@@ -744,6 +1502,52 @@ int mfg_boxlist_step(mfg_boxlist* L, double time, double dt, int mode, void* str
     return cudaGraphLaunch(L->gexec, st) == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
 }
 
+// The reference's multi-level step (subcycling, two-level fill with
+// conservative interpolation, flux registers, reflux, average_down).
+int mfg_boxlist_step_amr(mfg_boxlist* L, double time, double dt0, int mode, void* stream) {
+    if (!L || mode < 0 || mode > 2) return MFG_ERR_ARG;
+    if (L->amr_rc) return L->amr_rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (L->flux_tiles_kind != flux_kind(*L)) {
+        drop_graph(*L);
+        if (build_tiles(*L, L->ph[PH_FLUX], PH_FLUX, L->ph[PH_FLUX].tile_items, -1) != cudaSuccess)
+            return MFG_ERR_CUDA;
+    }
+    if (L->lt_version != L->tile_version || L->lt_flux_kind != flux_kind(*L)) {
+        drop_graph(*L);
+        if (build_level_tiles(*L) != cudaSuccess) return MFG_ERR_CUDA;
+    }
+    // coarse-data coefficients of this step's fills (host pass, then one upload;
+    // the kernels, and a captured graph, read them from device memory)
+    amr_run(*L, time, dt0, false, mode, st);
+    if (L->nevents &&
+        cudaMemcpyAsync(L->d_coef, L->hcoef.data(), L->nevents * sizeof(TCoef), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+        return MFG_ERR_CUDA;
+    if (mode < 2) return amr_run(*L, time, dt0, true, mode, st);
+    if (!L->gexec_amr || L->gdt_amr != dt0) {
+        if (L->gexec_amr) cudaGraphExecDestroy(L->gexec_amr);
+        L->gexec_amr = nullptr;
+        if (!st) return MFG_ERR_ARG;  // capture needs a non-default stream
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return MFG_ERR_CUDA;
+        const int rc = amr_run(*L, time, dt0, true, 1, st);
+        if (cudaStreamEndCapture(st, &g) != cudaSuccess || !g) return MFG_ERR_CUDA;
+        if (rc) {
+            cudaGraphDestroy(g);
+            return rc;
+        }
+        cudaError_t e = cudaGraphInstantiate(&L->gexec_amr, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            L->gexec_amr = nullptr;
+            return MFG_ERR_CUDA;
+        }
+        L->gdt_amr = dt0;
+    }
+    return cudaGraphLaunch(L->gexec_amr, st) == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
+
 // Measured search over tile size and grid size for each batched phase: every
 // candidate runs the phase alone (the phases are idempotent on their inputs:
 // fill, cut cells, face scalars, fluxes, and the update with stage 0, which only
@@ -776,7 +1580,7 @@ int mfg_boxlist_autotune(mfg_boxlist* L, double dt, double* results, void* strea
                     cudaEventRecord(e0, st);
                     switch (p) {
                         case PH_GROWN: b_fill(*L, P, 1, st); break;
-                        case PH_VALID: b_cutcells(*L, st); break;
+                        case PH_VALID: b_cutcells(*L, P, st); break;
                         case PH_FACE: {
                             NS_DISPATCH(bk_face, (P.grid, BT, 0, st), (L->d_rhs, P.d, P.n));
                             break;

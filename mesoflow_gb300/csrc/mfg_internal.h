@@ -29,7 +29,7 @@ enum KernelKind {
     K_PRIM = 0, K_FACE, K_FLUX, K_UPDATE, K_FILL_COPY, K_FILL_BC, K_CUT, K_CHEM, K_PRIMS, K_CLIP,
     K_RESNORM, K_TIMESTEP, K_COPY,
     // adjoint (mfg_adjoint.cu)
-    K_ADJ_FACE, K_ADJ_CELL, K_ADJ_CUT, K_ADJ_FILL, K_ADJ_LOCAL, K_SNAPSHOT, K_ADJ_FLUX, K_COUNT
+    K_ADJ_FACE, K_ADJ_CELL, K_ADJ_CUT, K_ADJ_FILL, K_ADJ_LOCAL, K_SNAPSHOT, K_ADJ_FLUX, K_AMR_SYNC, K_AMR_PATCH, K_AMR_INTERP, K_COUNT
 };
 
 // Counts one launch; when profiling is on, brackets it with CUDA events on its stream.

@@ -657,9 +657,9 @@ int build_registers(Amr& A, int l) {
                 const mfg_box& b = fl[fb];
                 const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
                 const int fface = side ? b.hi[d] + 1 : b.lo[d];
-                const int cface = fface / r;
-                for (int q2 = b.lo[t2] / r; q2 <= (b.hi[t2] + 1) / r - 1; q2++)
-                    for (int q1 = b.lo[t1] / r; q1 <= (b.hi[t1] + 1) / r - 1; q1++) {
+                const int cface = floor_div(fface, r);
+                for (int q2 = floor_div(b.lo[t2], r); q2 <= floor_div(b.hi[t2] + 1, r) - 1; q2++)
+                    for (int q1 = floor_div(b.lo[t1], r); q1 <= floor_div(b.hi[t1] + 1, r) - 1; q1++) {
                         int cc[3];
                         cc[d] = side ? cface : cface - 1;
                         cc[t1] = q1;
@@ -734,9 +734,9 @@ int average_down(Amr& A, int l) {  // level l+1 onto level l
     const std::vector<mfg_box>& cl = A.lv[l];
     for (const mfg_box& b : A.lv[l + 1]) {
         A4 f(b.s_new);
-        for (int k = b.lo[2] / r; k <= (b.hi[2] + 1) / r - 1; k++)
-            for (int j = b.lo[1] / r; j <= (b.hi[1] + 1) / r - 1; j++)
-                for (int i = b.lo[0] / r; i <= (b.hi[0] + 1) / r - 1; i++) {
+        for (int k = floor_div(b.lo[2], r); k <= floor_div(b.hi[2] + 1, r) - 1; k++)
+            for (int j = floor_div(b.lo[1], r); j <= floor_div(b.hi[1] + 1, r) - 1; j++)
+                for (int i = floor_div(b.lo[0], r); i <= floor_div(b.hi[0] + 1, r) - 1; i++) {
                     const int w[3] = {i, j, k};
                     const int cb = owner_of(cl.data(), (int)cl.size(), w);
                     if (cb < 0) return MFG_ERR_ARG;
