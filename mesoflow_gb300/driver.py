@@ -64,6 +64,38 @@ class Mflo:
     def state(self):
         return self.level.get_state(self.case.shape_zyx)
 
+    def _level_arrays(self):
+        import torch
+        torch.cuda.synchronize()
+        boxes = [(tuple(lo), tuple(hi)) for lo, hi in self.case.boxes]
+        return boxes, [a.detach().cpu().numpy() for a in self.level.s_new]
+
+    def write_plotfile(self, path, specnames=None):
+        """mflo::WritePlotFile (Source/mflo_plot.cpp:44-55) of this level."""
+        from . import plotfile
+        boxes, arrays = self._level_arrays()
+        plotfile.write_plotfile(path, [self.case.geom], [boxes], [arrays],
+                                plotfile.varnames(self.case.params.nspec, specnames), self.time, [self.istep])
+
+    def write_checkpoint(self, path, specnames=None):
+        """mflo::WriteCheckpointFile (Source/mflo_plot.cpp:57-145) of this level."""
+        from . import plotfile
+        boxes, arrays = self._level_arrays()
+        plotfile.write_checkpoint(path, [boxes], [arrays], plotfile.varnames(self.case.params.nspec, specnames),
+                                  [self.istep], [self.dt if self.dt < 1e100 else 0.0], [self.time])
+
+    def read_checkpoint(self, path, specnames=None):
+        """mflo::ReadCheckpointFile (Source/mflo_plot.cpp:147-240): restores the
+        state, time, step count and dt of a checkpoint of this box layout."""
+        import torch
+        from . import plotfile
+        r = plotfile.read_checkpoint(path, plotfile.varnames(self.case.params.nspec, specnames))
+        if r["finest_level"] != 0 or r["boxes"][0] != [(tuple(lo), tuple(hi)) for lo, hi in self.case.boxes]:
+            raise ValueError("checkpoint box layout differs from this level's")
+        for dst, src in zip(self.level.s_new, r["arrays"][0]):
+            dst.copy_(torch.as_tensor(src, device=dst.device))
+        self.istep, self.dt, self.time = r["istep"][0], r["dt"][0], r["t_new"][0]
+
     def status(self, clear=False):
         v = C.c_uint32()
         abi.check("mfg_status", self.lib.mfg_status(C.byref(v), int(clear)))
