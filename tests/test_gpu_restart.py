@@ -19,12 +19,12 @@ def test_checkpoint_restart_bitwise(tmp_path):
         a.advance()
     a.write_checkpoint(str(tmp_path / "chk00002"))
     a.write_plotfile(str(tmp_path / "plt00002"))
-    ref2 = a.state()
+    ref2, t2, dt2 = a.state(), a.time, a.dt
     for _ in range(2):
         a.advance()
     b = Mflo(c, device="cuda")
     b.read_checkpoint(str(tmp_path / "chk00002"))
-    assert b.istep == 2 and b.time == a.time - (a.time - b.time)
+    assert b.istep == 2 and b.time == t2 and b.dt == dt2
     assert np.array_equal(b.state(), ref2)
     for _ in range(2):
         b.advance()
