@@ -298,6 +298,29 @@ int mfg_set_weno_mode(int fast);
  * are bitwise the same either way.  enable = 0 frees the cache.  Synchronizes. */
 int mfg_set_cutcell_cache(int enable);
 
+/* ---- split-chemistry pieces (mflo::Evolve_split, Source/mflo_splitchem.cpp:24-72:
+ * flow to steady state, then chemistry sub-steps of the frozen flow, the flow
+ * variables brought back to the new concentrations, flow again) -------------- */
+
+/* mflo::Advance_chemistry (Source/mflo_splitchem.cpp:177-199): explicit
+ * midpoint step of the reaction source with the reference's phi_old/phi_new
+ * swap first, so the stage-1 source is evaluated on the incoming s_old and
+ * the stage-2 source on the midpoint: s_new <- s_new + dt F(s_new +
+ * dt/2 F(s_old)); on exit s_old holds the incoming s_new.  Asynchronous. */
+int mfg_chem_advance_rk2(const mfg_box* boxes, int nbox, double time, double dt, void* stream);
+
+/* mflo::store_inertgas_conc (Source/mflo_splitchem.cpp:150-175): in fluid
+ * cells the untracked background-gas concentration (thermo.H
+ * get_bgasconc_from_rc) goes to the density component.  Asynchronous. */
+int mfg_store_inertgas_conc(const mfg_box* boxes, int nbox, void* stream);
+
+/* mflo::update_vars_after_chemsolve (Source/mflo_splitchem.cpp:74-148): in
+ * fluid cells rho = get_r_from_c(species[, stored background gas when
+ * using_bg_inertgas]), momenta = rho x velocities, energy kept, primitives
+ * and temperature recomputed.  Synchronizes; MFG_ERR_NEG_PRESSURE where the
+ * reference aborts with "Pressure has gone negative". */
+int mfg_update_vars_after_chemsolve(const mfg_box* boxes, int nbox, int using_bg_inertgas, void* stream);
+
 /* Same result as mfg_compute_dsdt_flow, for callers that may not allocate
  * device memory (for example an AMReX application, whose arena reserves most
  * of the GPU at start-up, or a code with a fixed device-memory budget): the

@@ -110,6 +110,9 @@ SIGNATURES = [
     ("mfg_boxlist_destroy", C.c_int, [C.c_void_p]),
     ("mfg_boxlist_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
     ("mfg_boxlist_step_amr", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
+    ("mfg_chem_advance_rk2", C.c_int, [_BP, C.c_int, C.c_double, C.c_double, _VP]),
+    ("mfg_store_inertgas_conc", C.c_int, [_BP, C.c_int, _VP]),
+    ("mfg_update_vars_after_chemsolve", C.c_int, [_BP, C.c_int, C.c_int, _VP]),
     ("mfg_boxlist_autotune", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), _VP]),
     ("mfg_boxlist_cells", C.c_longlong, [C.c_void_p]),
     ("mfg_last_error", C.c_char_p, []),

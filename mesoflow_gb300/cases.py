@@ -296,7 +296,7 @@ def permeability(case, state):
 
 
 def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, block=True, u_in=1.0, dx=1e-5,
-             arrhenius=True):
+             arrhenius=True, bg_gas=False):
     """Catalyst block with explicit surface chemistry (models/stagFlowCatalyst /
     rxnscheme example pattern): 8 gas species + 2 non-advected site species
     (molar mixture, R = RU); mass-action surface reactions gas_a + site_b ->
@@ -304,7 +304,10 @@ def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, bloc
     or the reference's table form (Ea = 0) when arrhenius is False.
     Diffusivities blend gas/solid with vfrac; species_in_solid = 1.
     x: velocity inlet u_in / outflow (foextrap); y, z: walls.  The immersed
-    solid is a block in the middle third plus a seeded sphere pack."""
+    solid is a block in the middle third plus a seeded sphere pack.
+    bg_gas: the background-gas thermo family (rxnscheme example thermo.H): an
+    untracked inert gas (W = 0.028, gamma 1.4) holds 70% of the moles and the
+    tracked gases share the rest."""
     ng, nsite = 8, 2
     ns = ng + nsite
     P = _base_params(ns)
@@ -346,8 +349,15 @@ def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, bloc
     T, pres = 500.0, 1e5
     x = np.array([0.7, 0.1, 0.05, 0.05, 0.04, 0.03, 0.02, 0.01])
     ctot = pres / (RU * T)
+    cbg = 0.0
+    if bg_gas:
+        P.thermo_kind = abi.THERMO_BG_GAS
+        P.bg_molwt = 0.028
+        P.gamma[ng] = 1.4
+        cbg = 0.7 * ctot
+        x = 0.3 * x
     cg = x * ctot
-    rho_in = float(sum(cg[s] * W[s] for s in range(ng)))
+    rho_in = float(sum(cg[s] * W[s] for s in range(ng))) + cbg * P.bg_molwt
     P.bc_lo[0] = abi.BC_EXT_DIR
     P.bc_hi[0] = abi.BC_FOEXTRAP
     for d in (1, 2):
@@ -369,7 +379,7 @@ def catalyst(n=128, order=5, max_grid=32, seed=4, nreact=8, solid_frac=0.3, bloc
     spec = [np.full(shape, cg[s]) for s in range(ng)]
     site = np.where(vf < 1.0, 50.0, 0.0)
     spec += [site * 0.6, site * 0.4]
-    rho = sum(spec[s] * W[s] for s in range(ng))
+    rho = sum(spec[s] * W[s] for s in range(ng)) + cbg * P.bg_molwt
     u = np.where(vf == 1.0, u_in, 0.0)
     zero = np.zeros(shape)
     S = state_from_prim(P, rho, u, zero, zero, np.full(shape, pres), spec, vf)

@@ -358,6 +358,34 @@ int mfg_update_primitive_vars(const mfg_box* boxes, int nbox, const mfg_geom* ge
     return (after & MFG_STATUS_NEG_PRESSURE) ? MFG_ERR_NEG_PRESSURE : MFG_OK;
 }
 
+int mfg_chem_advance_rk2(const mfg_box* boxes, int nbox, double time, double dt, void* stream) {
+    (void)time;
+    int rc = check_boxes(boxes, nbox, false, false, true, true);
+    if (rc) return rc;
+    for (int b = 0; b < nbox; ++b)
+        if (launch_split_chem(boxes[b], 0, dt, 0, (cudaStream_t)stream) != cudaSuccess) return MFG_ERR_CUDA;
+    return MFG_OK;
+}
+
+int mfg_store_inertgas_conc(const mfg_box* boxes, int nbox, void* stream) {
+    int rc = check_boxes(boxes, nbox, false, false, false, true);
+    if (rc) return rc;
+    for (int b = 0; b < nbox; ++b)
+        if (launch_split_chem(boxes[b], 1, 0.0, 0, (cudaStream_t)stream) != cudaSuccess) return MFG_ERR_CUDA;
+    return MFG_OK;
+}
+
+int mfg_update_vars_after_chemsolve(const mfg_box* boxes, int nbox, int using_bg_inertgas, void* stream) {
+    int rc = check_boxes(boxes, nbox, false, false, false, true);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int b = 0; b < nbox; ++b)
+        if (launch_split_chem(boxes[b], 2, 0.0, using_bg_inertgas, st) != cudaSuccess) return MFG_ERR_CUDA;
+    unsigned after = 0;
+    if (cudaStreamSynchronize(st) != cudaSuccess || read_status(&after, false) != cudaSuccess) return MFG_ERR_CUDA;
+    return (after & MFG_STATUS_NEG_PRESSURE) ? MFG_ERR_NEG_PRESSURE : MFG_OK;
+}
+
 int mfg_clip_species(const mfg_box* boxes, int nbox, void* stream) {
     int rc = check_boxes(boxes, nbox, false, false, false, true);
     if (rc) return rc;

@@ -85,6 +85,7 @@ cudaError_t launch_chem_source(const mfg_box& b, cudaStream_t st);
 cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, double a, bool copy_first,
                               const Fab& base, int ncomp, cudaStream_t st);
 cudaError_t launch_update_prims(const mfg_box& b, double* minp_slot, cudaStream_t st);
+cudaError_t launch_split_chem(const mfg_box& b, int kind, double dt, int bg, cudaStream_t st);
 cudaError_t launch_clip_species(const mfg_box& b, cudaStream_t st);
 cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st);
 

@@ -36,6 +36,38 @@ __device__ __forceinline__ double thermo_t(double rho, double pres, const double
     return pres / (sum_ci * P.R_univ);
 }
 
+// Mixture density from the species concentrations (thermo.H get_r_from_c):
+// molar, catalystCylinder/thermo.H:37-45 (gas species); mass-single,
+// TaylorGreen/thermo.H:37-45 (every species); background gas, rxnscheme
+// example thermo.H:20-31 (gas species + bgasconc W_bg).
+template <int NS>
+__device__ __forceinline__ double thermo_r_from_c(const double* spec, double bgasconc) {
+    const DevParams& P = c_P;
+    const int n = (P.thermo_kind == MFG_THERMO_MASS_SINGLE) ? P.nspec : P.ngas;
+    double rho = 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < n) rho = add(rho, mul(spec[s], P.molwt[s]));
+    if (P.thermo_kind == MFG_THERMO_BG_GAS) rho = add(rho, mul(bgasconc, P.bg_molwt));
+    return rho;
+}
+
+// Untracked background-gas concentration (thermo.H get_bgasconc_from_rc):
+// molar 0 (catalystCylinder/thermo.H:47-52), mass-single the first species
+// (TaylorGreen/thermo.H:46-53), background gas (rho - sum c W) / W_bg
+// (rxnscheme example thermo.H:32-42).
+template <int NS>
+__device__ __forceinline__ double thermo_bgasconc(double rho, const double* spec) {
+    const DevParams& P = c_P;
+    if (P.thermo_kind == MFG_THERMO_MASS_SINGLE) return spec[0];
+    if (P.thermo_kind != MFG_THERMO_BG_GAS) return 0.0;
+    double sum_ciMi = 0.0;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < P.ngas) sum_ciMi = add(sum_ciMi, mul(spec[s], P.molwt[s]));
+    return __ddiv_rn(__dsub_rn(rho, sum_ciMi), P.bg_molwt);
+}
+
 // Pressure from (rho e, rho, species).
 template <int NS>
 __device__ __forceinline__ double thermo_p(double rhoe, double rho, const double* spec) {

@@ -19,6 +19,21 @@ template <int NS>
 __global__ void prims_kernel(Valid v, Fab S) {
     prims_body<NS>(v, S, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
+template <int NS>
+__global__ void chem_rk2_kernel(Valid v, Fab So, Fab Sn, double dt, int ncomp) {
+    chem_rk2_body<NS>(v, So, Sn, dt, ncomp, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <int NS>
+__global__ void inertgas_kernel(Valid v, Fab S) {
+    inertgas_body<NS>(v, S, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <int NS>
+__global__ void vars_after_chem_kernel(Valid v, Fab S, int bg) {
+    vars_after_chem_body<NS>(v, S, bg, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 __global__ void clip_kernel(Valid v, Fab S, int nspec) {
     clip_body(v, S, nspec, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -154,6 +169,27 @@ cudaError_t launch_update_prims(const mfg_box& b, double*, cudaStream_t st) {
     else if (ns <= 4) prims_kernel<4><<<nblocks(v.n), TPB, 0, st>>>(v, S);
     else if (ns <= 8) prims_kernel<8><<<nblocks(v.n), TPB, 0, st>>>(v, S);
     else prims_kernel<16><<<nblocks(v.n), TPB, 0, st>>>(v, S);
+    return cudaGetLastError();
+}
+
+// Split-chemistry pieces (Source/mflo_splitchem.cpp): kind 0 Advance_chemistry,
+// 1 store_inertgas_conc, 2 update_vars_after_chemsolve (bg = using_bg_inertgas).
+cudaError_t launch_split_chem(const mfg_box& b, int kind, double dt, int bg, cudaStream_t st) {
+    Valid v = valid_of(b);
+    Fab So = make_fab(b.s_old), Sn = make_fab(b.s_new);
+    const int ns = c_host_params().nspec, nc = NFLO + ns;
+    const unsigned g = nblocks(v.n);
+    ProfScope ps(K_CHEM, st);
+#define MFG_SPLIT(NSB)                                                                  \
+    if (kind == 0) chem_rk2_kernel<NSB><<<g, TPB, 0, st>>>(v, So, Sn, dt, nc);         \
+    else if (kind == 1) inertgas_kernel<NSB><<<g, TPB, 0, st>>>(v, Sn);                \
+    else vars_after_chem_kernel<NSB><<<g, TPB, 0, st>>>(v, Sn, bg);
+    if (ns <= 1) { MFG_SPLIT(1) }
+    else if (ns <= 2) { MFG_SPLIT(2) }
+    else if (ns <= 4) { MFG_SPLIT(4) }
+    else if (ns <= 8) { MFG_SPLIT(8) }
+    else { MFG_SPLIT(16) }
+#undef MFG_SPLIT
     return cudaGetLastError();
 }
 

@@ -115,6 +115,96 @@ __device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So,
     }
 }
 
+// mflo::Advance_chemistry (Source/mflo_splitchem.cpp:177-199), the explicit
+// midpoint chemistry step of the split driver.  The reference first swaps
+// phi_old and phi_new, so its stage-1 source is evaluated on the previous
+// phi_old (one chemistry step behind) and only the stage-2 source on the
+// midpoint:
+//   mid = 1*X + (dt/2) F(Y),  new = 1*X + dt F(mid),  X = s_new, Y = s_old;
+// on exit s_old = X, s_new = new.  F is the reaction source on the species
+// components and zero elsewhere (compute_dsdt_chemistry, :684-720), and the
+// LinComb runs over every component.
+template <int NS>
+__device__ __forceinline__ void chem_rk2_body(const Valid& v, const Fab& So, const Fab& Sn, double dt, int ncomp,
+                                              int64_t t) {
+    if (t >= v.n) return;
+    int i, j, k;
+    cell_of(v, t, i, j, k);
+    const int ns = c_P.nspec;
+    double y[NS], f[NS], m[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) y[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
+    spec_source<NS>(y, So(i, j, k, TEMP), f);
+    const double h = 0.5 * dt;
+    // midpoint: non-species components X + h*0, species X + h F(Y)
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        m[s] = (s < ns) ? add(mul(1.0, Sn(i, j, k, NFLO + s)), mul(h, add(0.0, add(0.0, f[s])))) : 0.0;
+    const double tmid = add(mul(1.0, Sn(i, j, k, TEMP)), mul(h, 0.0));
+    spec_source<NS>(m, tmid, f);
+    for (int n = 0; n < NFLO && n < ncomp; ++n) {
+        const double x = Sn(i, j, k, n);
+        So(i, j, k, n) = x;
+        Sn(i, j, k, n) = add(mul(1.0, x), mul(dt, 0.0));
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        if (s >= ns) continue;
+        const double x = Sn(i, j, k, NFLO + s);
+        So(i, j, k, NFLO + s) = x;
+        Sn(i, j, k, NFLO + s) = add(mul(1.0, x), mul(dt, add(0.0, add(0.0, f[s]))));
+    }
+}
+
+// mflo::store_inertgas_conc (Source/mflo_splitchem.cpp:150-175): fluid cells
+// keep the untracked background-gas concentration in the density slot while
+// the chemistry runs.
+template <int NS>
+__device__ __forceinline__ void inertgas_body(const Valid& v, const Fab& S, int64_t t) {
+    if (t >= v.n) return;
+    int i, j, k;
+    cell_of(v, t, i, j, k);
+    if (!(S(i, j, k, VFRAC) >= 1.0)) return;
+    double spec[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) spec[s] = (s < c_P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
+    S(i, j, k, DENS) = thermo_bgasconc<NS>(S(i, j, k, RHO), spec);
+}
+
+// mflo::update_vars_after_chemsolve (Source/mflo_splitchem.cpp:74-148): in
+// fluid cells the density follows the new concentrations (plus the stored
+// background gas when bg is set), the momenta follow density x the primitive
+// velocities, the energy is kept, and the primitives and temperature are
+// recomputed from the conserved state; negative pressure raises a status bit.
+template <int NS>
+__device__ __forceinline__ void vars_after_chem_body(const Valid& v, const Fab& S, int bg, int64_t t) {
+    if (t >= v.n) return;
+    int i, j, k;
+    cell_of(v, t, i, j, k);
+    const DevParams& P = c_P;
+    if (S(i, j, k, VFRAC) >= 1.0) {
+        double spec[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
+        const double rho = thermo_r_from_c<NS>(spec, bg ? S(i, j, k, DENS) : 0.0);
+        S(i, j, k, RHO) = rho;
+        S(i, j, k, DENS) = rho;
+        const double ru = mul(rho, S(i, j, k, VELX)), rv = mul(rho, S(i, j, k, VELY)), rw = mul(rho, S(i, j, k, VELZ));
+        S(i, j, k, RHOU) = ru;
+        S(i, j, k, RHOV) = rv;
+        S(i, j, k, RHOW) = rw;
+        const double vx = ru / rho, vy = rv / rho, vz = rw / rho;
+        const double rhoe = S(i, j, k, RHOE) - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
+        const double p = thermo_p<NS>(rhoe, rho, spec);
+        S(i, j, k, VELX) = vx;
+        S(i, j, k, VELY) = vy;
+        S(i, j, k, VELZ) = vz;
+        S(i, j, k, PRES) = p;
+        S(i, j, k, TEMP) = thermo_t<NS>(rho, p, spec);
+    }
+    if (P.do_ns && S(i, j, k, PRES) < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
+}
+
 // cons -> prim refresh (Source/mflo_evolve.cpp:114-171); negative pressure
 // raises a status bit instead of aborting.
 template <int NS>

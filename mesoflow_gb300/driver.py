@@ -47,19 +47,54 @@ class Mflo:
         self.dt = dt_new
         return dt_new
 
-    def advance(self, dt=None, norms=True):
+    def advance(self, dt=None, norms=True, only_flow=None):
         if dt is None:
             dt = self.compute_dt()
+        of = self.only_flow if only_flow is None else only_flow
         rn = (C.c_double * self.case.ncomp)()
         abi.check("mfg_advance_level",
                   self.lib.mfg_advance_level(self.desc, len(self.case.boxes), C.byref(self.case.geom), self.time,
-                                             dt, int(self.only_flow), int(self.clip), rn if norms else None,
+                                             dt, int(of), int(self.clip), rn if norms else None,
                                              C.c_void_p(self.stream)))
         if norms:
             self.resnorms = np.array(rn[:])
         self.time += dt
         self.istep += 1
         return dt
+
+    def evolve(self, final_time, only_flow=None, stop_time=1e300, max_step=10 ** 9, norms=False):
+        """mflo::EvolveAMR's loop (Source/mflo_evolve.cpp:18-89) for one level:
+        steps of ComputeDt + advance while time < final_time."""
+        while self.istep < max_step and self.time < final_time:
+            dt = self.compute_dt(stop_time)
+            self.advance(dt, norms=norms, only_flow=only_flow)
+            if self.time >= stop_time - 1e-6 * dt:
+                break
+
+    def evolve_split(self, t_ss, t_react, dt_react, dt_react_rk, dt_ss, bg_inertgas=False, stop_time=1e300,
+                     max_step=10 ** 9):
+        """mflo::Evolve_split (Source/mflo_splitchem.cpp:24-72), for slow
+        chemistry: the flow to t_ss (no chemistry), then until react_time
+        reaches t_react: chemistry sub-steps of dt_react_rk over dt_react on the
+        frozen flow (Advance_chemistry), the flow variables brought to the new
+        concentrations (update_vars_after_chemsolve), and dt_ss more of flow."""
+        st = C.c_void_p(self.stream)
+        n = len(self.case.boxes)
+        self.evolve(t_ss, only_flow=True, stop_time=stop_time, max_step=max_step)
+        flow_time, react_time = t_ss, 0.0
+        while react_time < t_react:
+            if bg_inertgas:
+                abi.check("mfg_store_inertgas_conc", self.lib.mfg_store_inertgas_conc(self.desc, n, st))
+            tchem = 0.0
+            while tchem < dt_react:
+                abi.check("mfg_chem_advance_rk2",
+                          self.lib.mfg_chem_advance_rk2(self.desc, n, react_time + tchem, dt_react_rk, st))
+                tchem += dt_react_rk
+            abi.check("mfg_update_vars_after_chemsolve",
+                      self.lib.mfg_update_vars_after_chemsolve(self.desc, n, int(bg_inertgas), st))
+            self.evolve(flow_time + dt_ss, only_flow=True, stop_time=stop_time, max_step=max_step)
+            react_time += dt_react
+            flow_time += dt_ss
 
     def state(self):
         return self.level.get_state(self.case.shape_zyx)

@@ -98,6 +98,29 @@ inline double get_t_from_rpc(const Ctx& c, double rho, double pres, const double
     return (pres / (sum_ci * P->R_univ));
 }
 
+// get_r_from_c: catalystCylinder/thermo.H:37-45 (molar, gas species),
+// TaylorGreen/thermo.H:37-45 (mass-single, every species), rxnscheme example
+// thermo.H:20-31 (background gas, + bgasconc W_bg).
+inline double get_r_from_c(const Ctx& c, const double* spec, double bgasconc) {
+    const mfg_params* P = c.P;
+    const int n = (P->thermo_kind == MFG_THERMO_MASS_SINGLE) ? P->nspec : P->ngas;
+    double rho = zeroval;
+    for (int sp = 0; sp < n; sp++) rho += spec[sp] * P->molwt[sp];
+    if (P->thermo_kind == MFG_THERMO_BG_GAS) rho += bgasconc * P->bg_molwt;
+    return rho;
+}
+
+// get_bgasconc_from_rc: catalystCylinder/thermo.H:47-52 (0), TaylorGreen/
+// thermo.H:46-53 (spec[AIR_ID]), rxnscheme example thermo.H:32-42.
+inline double get_bgasconc_from_rc(const Ctx& c, double rho, const double* spec) {
+    const mfg_params* P = c.P;
+    if (P->thermo_kind == MFG_THERMO_MASS_SINGLE) return spec[0];
+    if (P->thermo_kind != MFG_THERMO_BG_GAS) return 0.0;
+    double sum_ciMi = 0.0;
+    for (int sp = 0; sp < P->ngas; sp++) sum_ciMi += spec[sp] * P->molwt[sp];
+    return (rho - sum_ciMi) / P->bg_molwt;
+}
+
 inline double get_p_from_rec(const Ctx& c, double rhoe, double rho, const double* spec) {
     const mfg_params* P = c.P;
     if (P->thermo_kind == MFG_THERMO_MASS_SINGLE) {

@@ -956,6 +956,85 @@ int oracle_advance(const mfg_params* P, const mfg_geom* G, const mfg_box* boxes,
     return MFG_OK;
 }
 
+// mflo::Advance_chemistry (Source/mflo_splitchem.cpp:177-199), after its
+// swap: the stage-1 source on the incoming s_old, the midpoint
+// 1*X + (half dt) F in the s_new buffer, the stage-2 source there, then
+// s_new = 1*X + dt F; s_old ends holding X, the incoming s_new.
+int oracle_chem_advance_rk2(const mfg_params* P, const mfg_box* boxes, int nbox, double dt) {
+    Ctx c{P, P->nspec};
+    const int nc = ncomp_of(P);
+    for (int ib = 0; ib < nbox; ib++) {
+        const mfg_box& b = boxes[ib];
+        ValidFab X, F;
+        X.define(b, nc);
+        F.define(b, nc);
+        copy_valid(b, X.a, b.s_new, nc);
+        A4 x(X.a), f(F.a), sn(b.s_new);
+        chem_rhs_box(c, b, A4(b.s_old), f);  // compute_dsdt_chemistry(lev, .., S_new (= old phi_old))
+        copy_valid(b, b.s_old, X.a, nc);     // the swap: phi_old = current
+        for (int n = 0; n < nc; n++)
+            for (int k = b.lo[2]; k <= b.hi[2]; k++)
+                for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                    for (int i = b.lo[0]; i <= b.hi[0]; i++) sn(i, j, k, n) = one * x(i, j, k, n) + half * dt * f(i, j, k, n);
+        chem_rhs_box(c, b, sn, f);
+        for (int n = 0; n < nc; n++)
+            for (int k = b.lo[2]; k <= b.hi[2]; k++)
+                for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                    for (int i = b.lo[0]; i <= b.hi[0]; i++) sn(i, j, k, n) = one * x(i, j, k, n) + dt * f(i, j, k, n);
+    }
+    return MFG_OK;
+}
+
+// mflo::store_inertgas_conc (Source/mflo_splitchem.cpp:150-175).
+int oracle_store_inertgas_conc(const mfg_params* P, const mfg_box* boxes, int nbox) {
+    Ctx c{P, P->nspec};
+    for (int ib = 0; ib < nbox; ib++) {
+        const mfg_box& b = boxes[ib];
+        A4 s(b.s_new);
+        for (int k = b.lo[2]; k <= b.hi[2]; k++)
+            for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                for (int i = b.lo[0]; i <= b.hi[0]; i++) {
+                    if (!(s(i, j, k, VFRAC_INDX) >= one)) continue;
+                    double spec[MAXS];
+                    for (int sp = 0; sp < P->nspec; sp++) spec[sp] = s(i, j, k, FLO_NVARS + sp);
+                    s(i, j, k, DENS_INDX) = get_bgasconc_from_rc(c, s(i, j, k, RHO_INDX), spec);
+                }
+    }
+    return MFG_OK;
+}
+
+// mflo::update_vars_after_chemsolve (Source/mflo_splitchem.cpp:74-148).
+int oracle_update_vars_after_chemsolve(const mfg_params* P, const mfg_box* boxes, int nbox, int bg) {
+    Ctx c{P, P->nspec};
+    int status = MFG_OK;
+    for (int ib = 0; ib < nbox; ib++) {
+        const mfg_box& b = boxes[ib];
+        A4 s(b.s_new);
+        double minp = 1e300;
+        for (int k = b.lo[2]; k <= b.hi[2]; k++)
+            for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                for (int i = b.lo[0]; i <= b.hi[0]; i++) {
+                    if (s(i, j, k, VFRAC_INDX) >= one) {
+                        double spec[MAXS], u[MAXC], p[NCVARS];
+                        for (int sp = 0; sp < P->nspec; sp++) spec[sp] = s(i, j, k, sp + FLO_NVARS);
+                        s(i, j, k, RHO_INDX) = get_r_from_c(c, spec, bg ? s(i, j, k, DENS_INDX) : zeroval);
+                        s(i, j, k, DENS_INDX) = s(i, j, k, RHO_INDX);
+                        s(i, j, k, RHOU_INDX) = s(i, j, k, RHO_INDX) * s(i, j, k, VELX_INDX);
+                        s(i, j, k, RHOV_INDX) = s(i, j, k, RHO_INDX) * s(i, j, k, VELY_INDX);
+                        s(i, j, k, RHOW_INDX) = s(i, j, k, RHO_INDX) * s(i, j, k, VELZ_INDX);
+                        for (int q = 0; q < NCVARS; q++) u[q] = s(i, j, k, q + RHO_INDX);
+                        for (int q = 0; q < P->nspec; q++) u[q + NCVARS] = s(i, j, k, q + FLO_NVARS);
+                        cons_to_prim(c, u, p);
+                        for (int q = 0; q < NCVARS; q++) s(i, j, k, q + DENS_INDX) = p[q];
+                        s(i, j, k, TEMP_INDX) = get_t_from_rpc(c, s(i, j, k, DENS_INDX), s(i, j, k, PRES_INDX), u + NCVARS);
+                    }
+                    minp = std::min(minp, s(i, j, k, PRES_INDX));
+                }
+        if (minp < 0 && P->do_ns) status = MFG_ERR_NEG_PRESSURE;
+    }
+    return status;
+}
+
 // One coarse step of a multi-level run: the step body of mflo::EvolveAMR
 // (Source/mflo_evolve.cpp:26-58) around timeStep's subcycling (:174-247):
 // level l advances with dt0 / (ratio_1 ... ratio_l), its face fluxes feed the

@@ -44,6 +44,32 @@ class OracleLevel:
     def state(self):
         return self.level.get_state(self.case.shape_zyx)
 
+    # the loops of mflo::EvolveAMR and mflo::Evolve_split, as the driver runs them
+    def evolve(self, final_time, only_flow=False, stop_time=1e300):
+        while self.time < final_time:
+            dt = self.compute_dt(stop_time)
+            self.advance(dt, only_flow=only_flow)
+            if self.time >= stop_time - 1e-6 * dt:
+                break
+
+    def evolve_split(self, t_ss, t_react, dt_react, dt_react_rk, dt_ss, bg_inertgas=False):
+        P, n = C.byref(self.case.params), len(self.case.boxes)
+        self.evolve(t_ss, only_flow=True)
+        flow_time, react_time = t_ss, 0.0
+        while react_time < t_react:
+            if bg_inertgas:
+                assert self.lib.oracle_store_inertgas_conc(P, self.desc, n) == 0
+            tchem = 0.0
+            while tchem < dt_react:
+                assert self.lib.oracle_chem_advance_rk2(P, self.desc, n, dt_react_rk) == 0
+                tchem += dt_react_rk
+            rc = self.lib.oracle_update_vars_after_chemsolve(P, self.desc, n, int(bg_inertgas))
+            if rc != 0:
+                raise abi.MfloError("oracle_update_vars_after_chemsolve", rc)
+            self.evolve(flow_time + dt_ss, only_flow=True)
+            react_time += dt_react
+            flow_time += dt_ss
+
 
 class OracleAmr:
     """Multi-level runs of the oracle (subcycled coarse steps with flux

@@ -38,10 +38,12 @@ def small(name):
         return perturb(cases.catalyst(n=16, order=5, max_grid=8), 8, vel_amp=1e-2)
     if name == "cat2":
         return perturb(cases.catalyst(n=16, order=2, max_grid=8), 9, vel_amp=1e-2)
+    if name == "catbg5":
+        return perturb(cases.catalyst(n=16, order=5, max_grid=8, bg_gas=True), 10, vel_amp=1e-2)
     raise KeyError(name)
 
 
-NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2"]
+NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2", "catbg5"]
 
 
 class Gpu:
@@ -82,7 +84,7 @@ def test_fill_patch_bitwise(name):
         assert np.array_equal(np.nan_to_num(ob), np.nan_to_num(gb)) or rel_err(gb, ob)[0] < 1e-15, b
 
 
-@pytest.mark.parametrize("name", ["porous2", "porous5", "cat5"])
+@pytest.mark.parametrize("name", ["porous2", "porous5", "cat5", "catbg5"])
 def test_cutcells(name):
     c = small(name)
     o, g = oracle_for(c), Gpu(c)
@@ -140,7 +142,7 @@ def test_one_step_parity(name):
     assert np.all(np.abs(rg - ro) <= 1e-9 * np.abs(ro) + TOL_STEP * scale)
 
 
-@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5"])
+@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5", "catbg5"])
 def test_multistep_l2(name):
     c = small(name)
     o, g = oracle_for(c), Gpu(c)
@@ -155,7 +157,7 @@ def test_multistep_l2(name):
             assert np.linalg.norm(sg[comp] - so[comp]) / den < TOL_L2, comp
 
 
-@pytest.mark.parametrize("name", ["cat5"])
+@pytest.mark.parametrize("name", ["cat5", "catbg5"])
 def test_chemistry_parity(name):
     c = small(name)
     o, g = oracle_for(c), Gpu(c)
