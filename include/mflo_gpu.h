@@ -358,6 +358,21 @@ int mfg_boxlist_destroy(mfg_boxlist* list);
  * use and when dt changes; needs a non-default stream).  Asynchronous. */
 int mfg_boxlist_step(mfg_boxlist* list, double time, double dt, int mode, void* stream);
 
+/* mflo::EvolveAMR's loop on the device for the common-dt step of the list
+ * (Source/mflo_evolve.cpp:18-89; for one level exactly the reference's loop):
+ * while *istep < max_step and *time < final_time: ComputeDt (EstTimeStep of
+ * every level with cfl, at most 1.1 x the previous dt, the minimum over the
+ * levels, clamped so that time does not pass stop_time, mflo_timestep.cpp:
+ * 18-153), one batched step (as mfg_boxlist_step mode 1), time += dt; stop
+ * when time >= stop_time - 1e-6 dt or a NaN / negative-pressure status is
+ * raised.  The whole loop is one CUDA graph with a device-side loop condition:
+ * no step waits for the host.  *time, *dt (the previous step's dt; 1e100
+ * before the first step) and *istep are read and updated.  Needs a
+ * non-default stream and profiling off; synchronizes at the end; returns
+ * MFG_ERR_NAN / MFG_ERR_NEG_PRESSURE where the reference aborts. */
+int mfg_boxlist_evolve(mfg_boxlist* list, double final_time, double stop_time, int max_step, double* time,
+                       double* dt, int* istep, void* stream);
+
 /* One coarse step of the reference's multi-level time stepping over the whole
  * hierarchy (mflo::EvolveAMR's step, Source/mflo_evolve.cpp:26-58, and
  * mflo::timeStep, :174-247): level l advances with dt0 / (ratio_1 ... ratio_l)

@@ -110,6 +110,8 @@ SIGNATURES = [
     ("mfg_boxlist_destroy", C.c_int, [C.c_void_p]),
     ("mfg_boxlist_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
     ("mfg_boxlist_step_amr", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
+    ("mfg_boxlist_evolve", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int), _VP]),
     ("mfg_chem_advance_rk2", C.c_int, [_BP, C.c_int, C.c_double, C.c_double, _VP]),
     ("mfg_store_inertgas_conc", C.c_int, [_BP, C.c_int, _VP]),
     ("mfg_update_vars_after_chemsolve", C.c_int, [_BP, C.c_int, C.c_int, _VP]),

@@ -71,6 +71,16 @@ struct LevelG {
     int gran, mlen[3];
     long long owner_off;  // offset of this level's owner map in the concatenated map
     int ratio;            // refinement ratio to the coarser level
+    double dx[3];
+};
+
+// Device-resident state of mfg_boxlist_evolve's loop.
+constexpr int RUN_MAXLEV = 16;
+struct RunState {
+    double t, dt_prev, dt;
+    double final_time, stop_time, cfl;
+    int istep, max_step, nlev;
+    double acc[2 * RUN_MAXLEV];  // per level: max wave speed, max species diffusivity
 };
 
 enum Phase { PH_GROWN = 0, PH_VALID, PH_FACE, PH_FLUX, PH_UPDATE, PH_COUNT };
@@ -542,7 +552,8 @@ bool flux_sweep_mode() {
 }
 
 __global__ void __launch_bounds__(BT) bk_update(const RhsBox* __restrict__ B, const Tile* __restrict__ tiles,
-                                                int ntiles, int stage, double dt) {
+                                                int ntiles, int stage, double dt, const double* __restrict__ dtp) {
+    if (dtp) dt = *dtp;
     TILE_LOOP
     update_body(B[tl.box], stage, dt, tl.part, t);
     TILE_END
@@ -573,7 +584,8 @@ __global__ void __launch_bounds__(BT) bk_copy_old(const MBox* __restrict__ boxes
 
 template <int NS>
 __global__ void __launch_bounds__(BT) bk_chem(const MBox* __restrict__ boxes, const Tile* __restrict__ tiles,
-                                              int ntiles, double dt, int nc) {
+                                              int ntiles, double dt, int nc, const double* __restrict__ dtp) {
+    if (dtp) dt = *dtp;
     TILE_LOOP
     const MBox& b = boxes[tl.box];
     chem_substep_body<NS>(valid_mbox(b), b.sold, b.snew, dt, nc, t);
@@ -589,6 +601,83 @@ __global__ void __launch_bounds__(BT) bk_prims(const MBox* __restrict__ boxes, c
     prims_body<NS>(v, b.snew, t);
     if (clip) clip_body(v, b.snew, nspec, t);
     TILE_END
+}
+
+// EstTimeStep over the tile list of valid cells: per level, the maxima of the
+// wave speed and of the species diffusivity (one atomic per warp and tile).
+template <int NS>
+__global__ void __launch_bounds__(BT) bk_timestep(const MBox* __restrict__ boxes, const Tile* __restrict__ tiles,
+                                                  int ntiles, RunState* __restrict__ R) {
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+        const Tile tl = tiles[ti];
+        const MBox& b = boxes[tl.box];
+        const Valid v = valid_mbox(b);
+        double ws = 0.0, md = 0.0;
+        for (long long t = tl.start + threadIdx.x; t < tl.end; t += blockDim.x) {
+            int i, j, k;
+            cell_of(v, t, i, j, k);
+            double w1, m1;
+            timestep_cell<NS>(b.snew, i, j, k, w1, m1);
+            ws = fmax(ws, w1);
+            md = fmax(md, m1);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            ws = fmax(ws, __shfl_down_sync(0xffffffffu, ws, o));
+            md = fmax(md, __shfl_down_sync(0xffffffffu, md, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomic_max_nonneg(&R->acc[2 * b.level], ws);
+            atomic_max_nonneg(&R->acc[2 * b.level + 1], md);
+        }
+    }
+}
+
+// ComputeDt with one dt for every level (Source/mflo_timestep.cpp:18-50 with
+// no subcycling): per level EstTimeStep (:136-153) times cfl, capped at 1.1 x
+// the previous dt, the minimum over levels, clamped to stop_time.  The same
+// operations in the same order as the host path (mfg_est_timestep and the
+// driver's compute_dt).
+__global__ void bk_compute_dt(const LevelG* __restrict__ lev, RunState* __restrict__ R) {
+    double dt0 = 1.7976931348623157e308;
+    for (int l = 0; l < R->nlev; ++l) {
+        const double h0 = R->acc[2 * l], h1 = R->acc[2 * l + 1];
+        double est = 1.7976931348623157e308;
+        if (h0 > 0)
+            for (int d = 0; d < 3; ++d) est = dmin_(est, __ddiv_rn(lev[l].dx[d], h0));
+        if (h1 > 0)
+            for (int d = 0; d < 3; ++d)
+                est = dmin_(est, __ddiv_rn(__ddiv_rn(__dmul_rn(__dmul_rn(0.5, lev[l].dx[d]), lev[l].dx[d]), h1), 3.0));
+        est = __dmul_rn(est, R->cfl);
+        const double cap = __dmul_rn(1.1, R->dt_prev);
+        const double dtl = (cap < est) ? cap : est;
+        dt0 = dmin_(dt0, dtl);
+    }
+    const double eps = __dmul_rn(1e-3, dt0);
+    if (__dadd_rn(R->t, dt0) > __dsub_rn(R->stop_time, eps)) dt0 = __dsub_rn(R->stop_time, R->t);
+    R->dt = dt0;
+}
+
+// Loop condition of mfg_boxlist_evolve (mflo::EvolveAMR, Source/mflo_evolve.cpp:
+// 21-88): step count and final time, the stop-time break, and the status bits
+// where the reference aborts (NaN, negative pressure).
+__device__ __forceinline__ unsigned run_continue(const RunState* R) {
+    const unsigned bad = g_status & (MFG_STATUS_NAN | MFG_STATUS_NEG_PRESSURE);
+    return (R->istep < R->max_step && R->t < R->final_time && !bad) ? 1u : 0u;
+}
+
+__global__ void bk_run_init(RunState* __restrict__ R, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, run_continue(R));
+}
+
+__global__ void bk_run_advance(RunState* __restrict__ R, cudaGraphConditionalHandle h) {
+    const double dt = R->dt;
+    R->t = __dadd_rn(R->t, dt);
+    R->istep += 1;
+    R->dt_prev = dt;
+    for (int q = 0; q < 2 * RUN_MAXLEV; ++q) R->acc[q] = 0.0;
+    unsigned c = run_continue(R);
+    if (R->t >= __dsub_rn(R->stop_time, __dmul_rn(1e-6, dt))) c = 0u;
+    cudaGraphSetConditional(h, c);
 }
 
 #undef TILE_LOOP
@@ -654,6 +743,9 @@ struct mfg_boxlist {
     double gdt_amr = 0.0;
     int lt_flux_kind = -1;
     std::vector<int> h_owner;              // host copy of the owner maps
+    // device-resident time loop (mfg_boxlist_evolve)
+    RunState* d_run = nullptr;
+    cudaGraphExec_t gexec_run = nullptr;
 };
 
 namespace {
@@ -782,7 +874,7 @@ void b_cutcells(mfg_boxlist& L, const PhaseTiles& T, cudaStream_t st) {
     NS_DISPATCH(bk_cut, (L.cut_grid, BT, 0, st), (L.d_cut, L.d_cutlist, L.d_count));
 }
 
-void b_rhs(mfg_boxlist& L, const TSet& TS, int stage, double dt, cudaStream_t st) {
+void b_rhs(mfg_boxlist& L, const TSet& TS, int stage, double dt, cudaStream_t st, const double* dtp = nullptr) {
     const int ord = c_host_params().order_hyp;
     if (ord >= 4) {
         const PhaseTiles& T = TS[PH_GROWN];
@@ -809,11 +901,12 @@ void b_rhs(mfg_boxlist& L, const TSet& TS, int stage, double dt, cudaStream_t st
     {
         const PhaseTiles& T = TS[PH_UPDATE];
         ProfScope ps(K_UPDATE, st);
-        bk_update<<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n, stage, dt);
+        bk_update<<<T.grid, BT, 0, st>>>(L.d_rhs, T.d, T.n, stage, dt, dtp);
     }
 }
 
-void step_batched(mfg_boxlist& L, double dt, cudaStream_t st) {
+// dtp (optional): device address of dt (mfg_boxlist_evolve's loop).
+void step_batched(mfg_boxlist& L, double dt, cudaStream_t st, const double* dtp = nullptr) {
     const int nc = NFLO + c_host_params().nspec;
     const PhaseTiles& V = L.ph[PH_VALID];
     {
@@ -824,7 +917,7 @@ void step_batched(mfg_boxlist& L, double dt, cudaStream_t st) {
     for (int stage = 1; stage <= 3; ++stage) {
         b_fill(L, L.ph[PH_GROWN], stage == 1 ? 0 : 1, st);
         b_cutcells(L, L.ph[PH_VALID], st);
-        b_rhs(L, T, stage, dt, st);
+        b_rhs(L, T, stage, dt, st, dtp);
     }
     {
         ProfScope ps(K_COPY, st);
@@ -832,7 +925,7 @@ void step_batched(mfg_boxlist& L, double dt, cudaStream_t st) {
     }
     {
         ProfScope ps(K_CHEM, st);
-        NS_DISPATCH(bk_chem, (V.grid, BT, 0, st), (L.d_mbox, V.d, V.n, dt, nc));
+        NS_DISPATCH(bk_chem, (V.grid, BT, 0, st), (L.d_mbox, V.d, V.n, dt, nc, dtp));
     }
     {
         ProfScope ps(K_PRIMS, st);
@@ -875,6 +968,8 @@ void drop_graph(mfg_boxlist& L) {
     L.gexec = nullptr;
     if (L.gexec_amr) cudaGraphExecDestroy(L.gexec_amr);
     L.gexec_amr = nullptr;
+    if (L.gexec_run) cudaGraphExecDestroy(L.gexec_run);
+    L.gexec_run = nullptr;
 }
 
 // ---- multi-level step -------------------------------------------------------------
@@ -1213,7 +1308,7 @@ void amr_chem(mfg_boxlist& L, AmrRun& R, int l, double dtl) {
     const PhaseTiles& V = level_tiles(L, l)[PH_VALID];
     if (!V.n) return;
     ProfScope ps(K_CHEM, R.st);
-    NS_DISPATCH(bk_chem, (V.grid, BT, 0, R.st), (L.d_mbox, V.d, V.n, dtl, nc));
+    NS_DISPATCH(bk_chem, (V.grid, BT, 0, R.st), (L.d_mbox, V.d, V.n, dtl, nc, (const double*)nullptr));
 }
 
 void amr_sync(mfg_boxlist& L, AmrRun& R, int l) {  // reflux of level l, average_down of l+1 onto l
@@ -1385,6 +1480,7 @@ int mfg_boxlist_create(const mfg_box* boxes, int nbox, const mfg_geom* geoms, in
                 G.mlen[d] = (g.domain_hi[d] - g.domain_lo[d] + 1) / gr;
             }
             G.gran = gr;
+            for (int d = 0; d < 3; ++d) G.dx[d] = g.dx[d];
             G.owner_off = (long long)own.size();
             G.ratio = (l > 0) ? (int)((geoms[l - 1].dx[0] / g.dx[0]) + 0.5) : 1;
             const size_t base = own.size();
@@ -1454,6 +1550,7 @@ int mfg_boxlist_destroy(mfg_boxlist* L) {
     for (RegEnt* r : L->d_ent) cudaFree(r);
     cudaFree(L->d_cp);
     cudaFree(L->d_coef);
+    cudaFree(L->d_run);
     cudaFree(L->d_rhs);
     cudaFree(L->d_cut);
     cudaFree(L->d_mbox);
@@ -1500,6 +1597,88 @@ int mfg_boxlist_step(mfg_boxlist* L, double time, double dt, int mode, void* str
         L->gdt = dt;
     }
     return cudaGraphLaunch(L->gexec, st) == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
+}
+
+// mflo::EvolveAMR's loop on the device for the common-dt step: one CUDA graph
+// whose WHILE node repeats {EstTimeStep, ComputeDt, step, time += dt} while a
+// kernel-set condition holds, so no step waits for the host.
+int mfg_boxlist_evolve(mfg_boxlist* L, double final_time, double stop_time, int max_step, double* time, double* dt,
+                       int* istep, void* stream) {
+    if (!L || !time || !dt || !istep || !stream) return MFG_ERR_ARG;
+    if (L->nlev > RUN_MAXLEV) return MFG_ERR_ARG;
+    if (profile_enabled()) return MFG_ERR_STATE;  // event records cannot live in a conditional body
+    cudaStream_t st = (cudaStream_t)stream;
+    if (L->flux_tiles_kind != flux_kind(*L)) {
+        drop_graph(*L);
+        if (build_tiles(*L, L->ph[PH_FLUX], PH_FLUX, L->ph[PH_FLUX].tile_items, -1) != cudaSuccess)
+            return MFG_ERR_CUDA;
+    }
+    if (!L->d_run && cudaMalloc(&L->d_run, sizeof(RunState)) != cudaSuccess) return MFG_ERR_CUDA;
+    if (!L->gexec_run) {
+        cudaGraph_t g = nullptr;
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) return MFG_ERR_CUDA;
+        cudaGraphConditionalHandle h;
+        cudaGraphNode_t n0, wn;
+        cudaKernelNodeParams kp;
+        memset(&kp, 0, sizeof(kp));
+        RunState* R = L->d_run;
+        void* args[] = {&R, &h};
+        kp.func = (void*)bk_run_init;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = args;
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        bool ok = cudaGraphConditionalHandleCreate(&h, g, 0, 0) == cudaSuccess &&
+                  cudaGraphAddKernelNode(&n0, g, nullptr, 0, &kp) == cudaSuccess;
+        if (ok) {
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            ok = cudaGraphAddNode(&wn, g, &n0, nullptr, 1, &cp) == cudaSuccess;
+        }
+        if (ok) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess;
+            if (ok) {
+                const PhaseTiles& V = L->ph[PH_VALID];
+                NS_DISPATCH(bk_timestep, (V.grid, BT, 0, st), (L->d_mbox, V.d, V.n, R));
+                bk_compute_dt<<<1, 1, 0, st>>>(L->d_lev, R);
+                step_batched(*L, 0.0, st, &R->dt);
+                bk_run_advance<<<1, 1, 0, st>>>(R, h);
+                ok = cudaStreamEndCapture(st, &body) == cudaSuccess;
+            }
+        }
+        if (ok) ok = cudaGraphInstantiate(&L->gexec_run, g, 0) == cudaSuccess;
+        cudaGraphDestroy(g);
+        if (!ok) {
+            L->gexec_run = nullptr;
+            note_cuda_error(cudaGetLastError(), "building the device time loop");
+            return MFG_ERR_CUDA;
+        }
+    }
+    RunState hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.t = *time;
+    hs.dt_prev = *dt;
+    hs.final_time = final_time;
+    hs.stop_time = stop_time;
+    hs.cfl = c_host_params().cfl;
+    hs.istep = *istep;
+    hs.max_step = max_step;
+    hs.nlev = L->nlev;
+    if (cudaMemcpyAsync(L->d_run, &hs, sizeof(hs), cudaMemcpyHostToDevice, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaGraphLaunch(L->gexec_run, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaMemcpyAsync(&hs, L->d_run, sizeof(hs), cudaMemcpyDeviceToHost, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MFG_ERR_CUDA;
+    *time = hs.t;
+    *dt = hs.dt_prev;
+    *istep = hs.istep;
+    unsigned v = 0;
+    if (read_status(&v, false) != cudaSuccess) return MFG_ERR_CUDA;
+    if (v & MFG_STATUS_NAN) return MFG_ERR_NAN;
+    if (v & MFG_STATUS_NEG_PRESSURE) return MFG_ERR_NEG_PRESSURE;
+    return MFG_OK;
 }
 
 // The reference's multi-level step (subcycling, two-level fill with
@@ -1593,7 +1772,7 @@ int mfg_boxlist_autotune(mfg_boxlist* L, double dt, double* results, void* strea
                             else
                                 bk_flux<true><<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n);
                             break;
-                        case PH_UPDATE: bk_update<<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n, 0, dt); break;
+                        case PH_UPDATE: bk_update<<<P.grid, BT, 0, st>>>(L->d_rhs, P.d, P.n, 0, dt, nullptr); break;
                     }
                     cudaEventRecord(e1, st);
                     cudaEventSynchronize(e1);

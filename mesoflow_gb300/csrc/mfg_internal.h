@@ -33,6 +33,9 @@ enum KernelKind {
 };
 
 // Counts one launch; when profiling is on, brackets it with CUDA events on its stream.
+// True while mfg_profile is on (per-launch CUDA events are recorded).
+bool profile_enabled();
+
 class ProfScope {
   public:
     ProfScope(int kind, cudaStream_t st);

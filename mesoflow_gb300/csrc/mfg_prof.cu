@@ -50,6 +50,8 @@ void drain() {
 
 }  // namespace
 
+bool profile_enabled() { return g_on; }
+
 ProfScope::ProfScope(int kind, cudaStream_t st) : kind_(kind), st_(st), a_(nullptr) {
     ++g_launches;
     if (g_on) {

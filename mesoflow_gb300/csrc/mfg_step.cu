@@ -71,10 +71,6 @@ __global__ void resnorm_final_kernel(const double* partial, int nblk, double* ac
     if (threadIdx.x == 0) acc[n] += x;
 }
 
-__device__ __forceinline__ void atomic_max_nonneg(double* a, double v) {
-    // IEEE order of non-negative doubles equals the order of their bit patterns
-    atomicMax(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double_as_longlong(v));
-}
 
 // max wavespeed and max species diffusivity (Source/mflo_timestep.cpp:83-133)
 template <int NS>
@@ -84,25 +80,7 @@ __global__ void timestep_kernel(Valid v, Fab S, double* acc2) {
     if (t < v.n) {
         int i, j, k;
         cell_of(v, t, i, j, k);
-        const DevParams& P = c_P;
-        const double vf = S(i, j, k, VFRAC);
-        if (vf > 0.0) {
-            const double ux = S(i, j, k, VELX), uy = S(i, j, k, VELY), uz = S(i, j, k, VELZ);
-            const double fsp = sqrt((ux * ux + uy * uy) + uz * uz);
-            double spec[NS];
-#pragma unroll
-            for (int s = 0; s < NS; ++s) spec[s] = (s < P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
-            const double gam = thermo_gamma<NS>(S(i, j, k, DENS), spec);
-            const double ss = sqrt((gam * S(i, j, k, PRES)) / S(i, j, k, DENS));
-            ws = fsp + (double)P.do_ns * ss;
-        }
-        double m = blend(P.diff_mode[0], P.diff_gas[0], P.diff_solid[0], vf);
-        for (int s = 0; s < P.nspec; ++s) {
-            const double dd = blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf);
-            if (dd > m) m = dd;
-        }
-        md = fabs(m);
-        ws = fabs(ws);
+        timestep_cell<NS>(S, i, j, k, ws, md);
     }
     for (int o = 16; o > 0; o >>= 1) {
         ws = fmax(ws, __shfl_down_sync(0xffffffffu, ws, o));

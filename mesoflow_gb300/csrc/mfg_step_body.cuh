@@ -234,6 +234,37 @@ __device__ __forceinline__ void prims_body(const Valid& v, const Fab& S, int64_t
     if (P.do_ns && S(i, j, k, PRES) < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
 }
 
+__device__ __forceinline__ void atomic_max_nonneg(double* a, double v) {
+    // IEEE order of non-negative doubles equals the order of their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double_as_longlong(v));
+}
+
+// One cell's wave speed |u| + do_ns c and largest species diffusivity
+// (EstTimeStep, Source/mflo_timestep.cpp:83-133), both non-negative.
+template <int NS>
+__device__ __forceinline__ void timestep_cell(const Fab& S, int i, int j, int k, double& ws, double& md) {
+    const DevParams& P = c_P;
+    ws = 0.0;
+    const double vf = S(i, j, k, VFRAC);
+    if (vf > 0.0) {
+        const double ux = S(i, j, k, VELX), uy = S(i, j, k, VELY), uz = S(i, j, k, VELZ);
+        const double fsp = sqrt((ux * ux + uy * uy) + uz * uz);
+        double spec[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
+        const double gam = thermo_gamma<NS>(S(i, j, k, DENS), spec);
+        const double ss = sqrt((gam * S(i, j, k, PRES)) / S(i, j, k, DENS));
+        ws = fsp + (double)P.do_ns * ss;
+    }
+    double m = blend(P.diff_mode[0], P.diff_gas[0], P.diff_solid[0], vf);
+    for (int s = 0; s < P.nspec; ++s) {
+        const double dd = blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf);
+        if (dd > m) m = dd;
+    }
+    md = fabs(m);
+    ws = fabs(ws);
+}
+
 __device__ __forceinline__ void clip_body(const Valid& v, const Fab& S, int nspec, int64_t t) {
     if (t >= v.n) return;
     int i, j, k;

@@ -201,3 +201,55 @@ def test_amr_rejects_unnested_hierarchy():
     s = torch.cuda.Stream()
     assert lib.mfg_boxlist_step_amr(h, 0.0, 2e-9, 1, C.c_void_p(s.cuda_stream)) == abi.ERR_ARG
     lib.mfg_boxlist_destroy(h)
+
+
+@pytest.mark.parametrize("name", ["cat5", "porous2"])
+def test_device_time_loop_equals_host_loop(name):
+    """mfg_boxlist_evolve (ComputeDt, step and loop condition on the device, one
+    graph launch) gives bitwise the states, time, dt and step count of the host
+    loop of ComputeDt (mfg_est_timestep, change_max 1.1, stop-time clamp) and
+    batched steps, including the final step clamped to the stop time."""
+    from helpers import perturb as _p
+    c = _p(cases.catalyst(n=24, order=5, max_grid=12), 31, vel_amp=1e-2) if name == "cat5" else \
+        _p(cases.porous_ib(n=24, order=2, max_grid=12), 32, vel_amp=1e-2)
+    lib = abi.load()
+    abi.check("mfg_init", lib.mfg_init(C.byref(c.params)))
+    s = torch.cuda.Stream()
+    st = C.c_void_p(s.cuda_stream)
+    geoms = (abi.Geom * 1)(c.geom)
+    a = Level(c.boxes, c.ncomp, backend="torch", device="cuda")
+    b = Level(c.boxes, c.ncomp, backend="torch", device="cuda")
+    a.set_state(c.state)
+    b.set_state(c.state)
+    ha = _boxlist(lib, a.descriptors(), len(c.boxes), geoms, 1)
+    hb = _boxlist(lib, b.descriptors(), len(c.boxes), geoms, 1)
+    # host loop
+    t, dtp, n = 0.0, 1e100, 0
+    with torch.cuda.stream(s):
+        est = C.c_double()
+        abi.check("est", lib.mfg_est_timestep(a.descriptors(), len(c.boxes), C.byref(c.geom), t, C.byref(est), st))
+    stop = 4.5 * est.value
+    with torch.cuda.stream(s):
+        while n < 10 and t < stop:
+            abi.check("est", lib.mfg_est_timestep(a.descriptors(), len(c.boxes), C.byref(c.geom), t,
+                                                  C.byref(est), st))
+            dt = min(est.value, 1.1 * dtp)
+            if t + dt > stop - 1e-3 * dt:
+                dt = stop - t
+            abi.check("step", lib.mfg_boxlist_step(ha, t, dt, 1, st))
+            t += dt
+            n += 1
+            dtp = dt
+            if t >= stop - 1e-6 * dt:
+                break
+    s.synchronize()
+    # device loop
+    tt, dd, nn = C.c_double(0.0), C.c_double(1e100), C.c_int(0)
+    with torch.cuda.stream(s):
+        abi.check("evolve", lib.mfg_boxlist_evolve(hb, 1e300, stop, 10, C.byref(tt), C.byref(dd), C.byref(nn), st))
+    s.synchronize()
+    lib.mfg_boxlist_destroy(ha)
+    lib.mfg_boxlist_destroy(hb)
+    assert nn.value == n and tt.value == t and dd.value == dtp, (nn.value, n, tt.value, t)
+    assert n >= 5
+    assert np.array_equal(a.get_state(c.shape_zyx), b.get_state(c.shape_zyx))
