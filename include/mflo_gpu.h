@@ -77,6 +77,7 @@ extern "C" {
 #define MFG_STATUS_NEG_PRESSURE  0x2u
 #define MFG_STATUS_TIMEOUT       0x4u
 #define MFG_STATUS_BAD_BOX       0x8u
+#define MFG_STATUS_CHEM_STEPS    0x10u  /* implicit chemistry needed more than max_substeps in a cell */
 
 /* ---- thermo / transport / boundary enums ---------------------------------- */
 /* thermo families found in the reference's per-case thermo.H plugins */
@@ -297,6 +298,18 @@ int mfg_set_weno_mode(int fast);
  * to recomputation in the same call and is dropped from the cache.  Results
  * are bitwise the same either way.  enable = 0 frees the cache.  Synchronizes. */
 int mfg_set_cutcell_cache(int enable);
+
+/* Integrator of the chemistry sub-step (mfg_chem_substep, mfg_advance_level,
+ * the box-list steps): kind 0 (default) the explicit SSP-RK3 of the
+ * reference's AMReX TimeIntegrator (rk.type 3); kind 1 an implicit, L-stable,
+ * adaptive second-order Rosenbrock method (ROS2, gamma = 1 + 1/sqrt 2, with
+ * the analytic Jacobian of the mass-action source and the embedded
+ * first-order error estimate, error norm RMS(err / (atol + rtol max|c|)))
+ * for stiff chemistry, where the reference uses SUNDIALS CVODE
+ * (integration.type = SUNDIALS, Source/mflo_evolve.cpp:455-469), which is not
+ * available here.  A cell that needs more than max_substeps substeps raises
+ * MFG_STATUS_CHEM_STEPS.  Applies from the next launch, kept across mfg_init. */
+int mfg_set_chem_integrator(int kind, double rtol, double atol, int max_substeps);
 
 /* ---- split-chemistry pieces (mflo::Evolve_split, Source/mflo_splitchem.cpp:24-72:
  * flow to steady state, then chemistry sub-steps of the frozen flow, the flow

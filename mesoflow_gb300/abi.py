@@ -17,7 +17,7 @@ DENS, VELX, VELY, VELZ, PRES, TEMP, VFRAC = 5, 6, 7, 8, 9, 10, 11
 
 OK, ERR_ARG, ERR_NAN, ERR_NEG_PRESSURE, ERR_SCHEME, ERR_TIMEOUT, ERR_CUDA, ERR_STATE, ERR_SIZE = range(9)
 NOALLOC_SCRATCH_DOUBLES = 4194304
-STATUS_NAN, STATUS_NEG_PRESSURE, STATUS_TIMEOUT, STATUS_BAD_BOX = 0x1, 0x2, 0x4, 0x8
+STATUS_NAN, STATUS_NEG_PRESSURE, STATUS_TIMEOUT, STATUS_BAD_BOX, STATUS_CHEM_STEPS = 0x1, 0x2, 0x4, 0x8, 0x10
 
 THERMO_MOLAR, THERMO_MASS_SINGLE, THERMO_BG_GAS = 0, 1, 2
 EFORM_MOLAR_CV, EFORM_MASS_CV = 0, 1
@@ -113,6 +113,7 @@ SIGNATURES = [
     ("mfg_boxlist_evolve", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int), _VP]),
     ("mfg_chem_advance_rk2", C.c_int, [_BP, C.c_int, C.c_double, C.c_double, _VP]),
+    ("mfg_set_chem_integrator", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_int]),
     ("mfg_store_inertgas_conc", C.c_int, [_BP, C.c_int, _VP]),
     ("mfg_update_vars_after_chemsolve", C.c_int, [_BP, C.c_int, C.c_int, _VP]),
     ("mfg_boxlist_autotune", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), _VP]),

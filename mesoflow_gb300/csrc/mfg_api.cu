@@ -19,6 +19,11 @@ void fill_release();
 namespace {
 
 DevParams g_hp;
+// chemistry integrator settings (mfg_set_chem_integrator), kept across mfg_init
+struct ChemSettings {
+    int kind = 0, maxsub = 1000;
+    double rtol = 1e-8, atol = 1e-12;
+} g_chem;
 bool g_ready = false;
 bool g_fast_weno = true;
 
@@ -245,10 +250,28 @@ int mfg_init(const mfg_params* p) {
         h.ext_lo[d] = p->ext_lo[d];
         h.ext_hi[d] = p->ext_hi[d];
     }
+    h.chem_kind = g_chem.kind;
+    h.chem_maxsub = g_chem.maxsub;
+    h.chem_rtol = g_chem.rtol;
+    h.chem_atol = g_chem.atol;
     if (upload_params(h) != cudaSuccess) return MFG_ERR_CUDA;
     g_hp = h;
     g_ready = true;
     return MFG_OK;
+}
+
+int mfg_set_chem_integrator(int kind, double rtol, double atol, int max_substeps) {
+    if (kind < 0 || kind > 1 || !(rtol > 0.0) || !(atol > 0.0) || max_substeps < 1) return MFG_ERR_ARG;
+    g_chem.kind = kind;
+    g_chem.rtol = rtol;
+    g_chem.atol = atol;
+    g_chem.maxsub = max_substeps;
+    if (!g_ready) return MFG_OK;
+    g_hp.chem_kind = kind;
+    g_hp.chem_rtol = rtol;
+    g_hp.chem_atol = atol;
+    g_hp.chem_maxsub = max_substeps;
+    return upload_params(g_hp) == cudaSuccess ? MFG_OK : MFG_ERR_CUDA;
 }
 
 int mfg_finalize(void) {

@@ -51,6 +51,9 @@ struct DevParams {
     // sparsity of the reaction table as bit masks over the species (bit s:
     // order[r][s] > 0, resp. nu[r][s] != 0), so the kernels test integers
     unsigned ord_mask[MAXR], nu_mask[MAXR];
+    // chemistry sub-step integrator: 0 SSP-RK3 (the reference's default), 1 adaptive ROS2
+    int chem_kind, chem_maxsub;
+    double chem_rtol, chem_atol;
     int bc_lo[3], bc_hi[3];
     mfg_extbc ext_lo[3], ext_hi[3];
 };

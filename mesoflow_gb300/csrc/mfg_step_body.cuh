@@ -74,6 +74,144 @@ __device__ __forceinline__ void chem_source_body(const Valid& v, const Fab& S, c
         if (s < c_P.nspec) D(i, j, k, NFLO + s) = add(D(i, j, k, NFLO + s), add(0.0, w[s]));
 }
 
+// Reaction source and its Jacobian d wdot_s / d c_q (mass action: the
+// derivative of c^o is 1 for o = 1, 2c for o = 2, o c^(o-1) otherwise).
+template <int NS>
+__device__ __forceinline__ void spec_source_jac(const double* spec, double temp, double* wdot, double (*J)[NS]) {
+    const DevParams& P = c_P;
+    const int ns = P.nspec;
+    for (int s = 0; s < ns; ++s) {
+        wdot[s] = 0.0;
+        for (int q = 0; q < ns; ++q) J[s][q] = 0.0;
+    }
+    if (!P.chem_on) return;
+    for (int r = 0; r < P.nreact; ++r) {
+        double kr = P.A[r];
+        if (P.Ea[r] != 0.0) kr = P.A[r] * exp(-P.Ea[r] / (kRU * temp));
+        double cm = 1.0;
+        for (int s = 0; s < ns; ++s) {
+            if (!((P.ord_mask[r] >> s) & 1u)) continue;
+            const double o = P.order[r][s], c = spec[s];
+            cm *= (o == 1.0) ? c : (o == 2.0) ? c * c : pow(c, o);
+        }
+        const double rate = kr * cm;
+        for (int s = 0; s < ns; ++s)
+            if ((P.nu_mask[r] >> s) & 1u) wdot[s] += P.nu[r][s] * rate;
+        for (int q = 0; q < ns; ++q) {
+            if (!((P.ord_mask[r] >> q) & 1u)) continue;
+            double dr = kr;
+            for (int p = 0; p < ns; ++p) {
+                if (!((P.ord_mask[r] >> p) & 1u)) continue;
+                const double o = P.order[r][p], c = spec[p];
+                if (p == q)
+                    dr *= (o == 1.0) ? 1.0 : (o == 2.0) ? 2.0 * c : o * pow(c, o - 1.0);
+                else
+                    dr *= (o == 1.0) ? c : (o == 2.0) ? c * c : pow(c, o);
+            }
+            for (int s = 0; s < ns; ++s)
+                if ((P.nu_mask[r] >> s) & 1u) J[s][q] += P.nu[r][s] * dr;
+        }
+    }
+}
+
+// Solves W x = b in place (b -> x) for the LU factors of W (unit lower, upper,
+// row exchanges piv) from lu_factor.
+template <int NS>
+__device__ __forceinline__ void lu_factor(double (*W)[NS], int* piv, int n) {
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        double amax = fabs(W[k][k]);
+        for (int i = k + 1; i < n; ++i)
+            if (fabs(W[i][k]) > amax) {
+                amax = fabs(W[i][k]);
+                p = i;
+            }
+        piv[k] = p;
+        if (p != k)
+            for (int j = 0; j < n; ++j) {
+                const double t = W[k][j];
+                W[k][j] = W[p][j];
+                W[p][j] = t;
+            }
+        const double ip = 1.0 / W[k][k];
+        for (int i = k + 1; i < n; ++i) {
+            const double l = W[i][k] * ip;
+            W[i][k] = l;
+            for (int j = k + 1; j < n; ++j) W[i][j] -= l * W[k][j];
+        }
+    }
+}
+
+template <int NS>
+__device__ __forceinline__ void lu_solve(const double (*W)[NS], const int* piv, int n, double* b) {
+    for (int k = 0; k < n; ++k)
+        if (piv[k] != k) {
+            const double t = b[k];
+            b[k] = b[piv[k]];
+            b[piv[k]] = t;
+        }
+    for (int i = 1; i < n; ++i)
+        for (int j = 0; j < i; ++j) b[i] -= W[i][j] * b[j];
+    for (int i = n - 1; i >= 0; --i) {
+        for (int j = i + 1; j < n; ++j) b[i] -= W[i][j] * b[j];
+        b[i] /= W[i][i];
+    }
+}
+
+// Implicit chemistry of one cell over dt: ROS2 (Verwer et al. 1999), L-stable,
+//   (I - g h J) k1 = f(y),  (I - g h J) k2 = f(y + h k1) - 2 k1,
+//   y+ = y + 3/2 h k1 + 1/2 h k2,  g = 1 + 1/sqrt(2),
+// with the embedded first-order error y+ - (y + h k1) = h (k1 + k2) / 2, the
+// RMS norm of err / (atol + rtol max(|y|, |y+|)), acceptance at <= 1 and the
+// step factor min(5, max(0.2, 0.9 / sqrt(norm))).  Returns false (and raises
+// MFG_STATUS_CHEM_STEPS) after chem_maxsub attempts.
+template <int NS>
+__device__ bool chem_ros2_cell(double* y, double temp, double dt) {
+    const DevParams& P = c_P;
+    const int ns = P.nspec;
+    const double g = 1.7071067811865475;
+    double W[NS][NS], f0[NS], k1[NS], k2[NS], y1[NS];
+    int piv[NS];
+    double t = 0.0, h = dt;
+    for (int att = 0; att < P.chem_maxsub; ++att) {
+        bool last = false;
+        if (t + h >= dt) {
+            h = dt - t;
+            last = true;
+        }
+        spec_source_jac<NS>(y, temp, f0, W);
+        for (int s = 0; s < ns; ++s) {
+            for (int q = 0; q < ns; ++q) W[s][q] = -(g * h) * W[s][q];
+            W[s][s] += 1.0;
+        }
+        lu_factor<NS>(W, piv, ns);
+        for (int s = 0; s < ns; ++s) k1[s] = f0[s];
+        lu_solve<NS>(W, piv, ns, k1);
+        for (int s = 0; s < ns; ++s) y1[s] = y[s] + h * k1[s];
+        spec_source<NS>(y1, temp, k2);
+        for (int s = 0; s < ns; ++s) k2[s] -= 2.0 * k1[s];
+        lu_solve<NS>(W, piv, ns, k2);
+        double e2 = 0.0;
+        for (int s = 0; s < ns; ++s) {
+            const double yn = y[s] + (1.5 * h) * k1[s] + (0.5 * h) * k2[s];
+            const double err = (0.5 * h) * (k1[s] + k2[s]);
+            const double sc = P.chem_atol + P.chem_rtol * fmax(fabs(y[s]), fabs(yn));
+            e2 += (err / sc) * (err / sc);
+            y1[s] = yn;
+        }
+        const double en = sqrt(e2 / (double)ns);
+        if (en <= 1.0) {
+            for (int s = 0; s < ns; ++s) y[s] = y1[s];
+            t += h;
+            if (last) return true;
+        }
+        const double fac = (en > 0.0) ? fmin(5.0, fmax(0.2, 0.9 / sqrt(en))) : 5.0;
+        h *= fac;
+    }
+    raise_status(MFG_STATUS_CHEM_STEPS);
+    return false;
+}
+
 // SSP-RK3 sub-step of the reaction source for one cell, all three stages in
 // registers (the chemistry right-hand side is local to the cell).  Stage
 // states S_i = S_old + sum_j (dt*a_ij) F_j, result S_old + sum_i (dt*w_i) F_i
@@ -86,6 +224,18 @@ __device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So,
     int i, j, k;
     cell_of(v, t, i, j, k);
     const int ns = c_P.nspec;
+    if (c_P.chem_kind == 1) {  // implicit (ROS2) chemistry
+        double y[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) y[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
+        chem_ros2_cell<NS>(y, So(i, j, k, TEMP), dt);
+        for (int n = 0; n < ncomp; ++n) {
+            if (n >= NFLO) continue;
+            Sn(i, j, k, n) = So(i, j, k, n);
+        }
+        for (int s = 0; s < ns; ++s) Sn(i, j, k, NFLO + s) = y[s];
+        return;
+    }
     double s0[NS], s1[NS], f0[NS], f1[NS], f2[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) s0[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;

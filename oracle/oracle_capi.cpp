@@ -956,6 +956,111 @@ int oracle_advance(const mfg_params* P, const mfg_geom* G, const mfg_box* boxes,
     return MFG_OK;
 }
 
+// Implicit chemistry sub-step (the product's ROS2 option, which stands in for
+// the reference's SUNDIALS CVODE path): per cell, over dt, the adaptive
+// second-order Rosenbrock method with the analytic mass-action Jacobian,
+// restated from Verwer et al. (1999) with the same step control as the
+// product: RMS error norm of h (k1 + k2)/2 against atol + rtol max(|y|, |y+|),
+// accept at <= 1, factor min(5, max(0.2, 0.9/sqrt(norm))).  Returns
+// MFG_ERR_TIMEOUT if a cell needs more than maxsub attempts.
+int oracle_chem_substep_ros2(const mfg_params* P, const mfg_box* boxes, int nbox, double dt, double rtol,
+                             double atol, int maxsub) {
+    Ctx c{P, P->nspec};
+    const int ns = P->nspec, nc = ncomp_of(P);
+    const double g = 1.0 + 1.0 / std::sqrt(2.0);
+    int status = MFG_OK;
+    for (int ib = 0; ib < nbox; ib++) {
+        const mfg_box& b = boxes[ib];
+        A4 so(b.s_old), sn(b.s_new);
+        for (int k = b.lo[2]; k <= b.hi[2]; k++)
+            for (int j = b.lo[1]; j <= b.hi[1]; j++)
+                for (int i = b.lo[0]; i <= b.hi[0]; i++) {
+                    for (int n = 0; n < FLO_NVARS && n < nc; n++) sn(i, j, k, n) = so(i, j, k, n);
+                    const double temp = so(i, j, k, TEMP_INDX);
+                    double y[MAXS], f0[MAXS], k1[MAXS], k2[MAXS], y1[MAXS], W[MAXS][MAXS];
+                    int piv[MAXS];
+                    for (int s = 0; s < ns; s++) y[s] = so(i, j, k, FLO_NVARS + s);
+                    double t = 0.0, h = dt;
+                    bool done = false;
+                    for (int att = 0; att < maxsub && !done; att++) {
+                        bool last = false;
+                        if (t + h >= dt) { h = dt - t; last = true; }
+                        // source and Jacobian
+                        compute_spec_source(c, y, temp, f0);
+                        for (int s = 0; s < ns; s++)
+                            for (int q = 0; q < ns; q++) W[s][q] = 0.0;
+                        if (P->chem_on)
+                            for (int r = 0; r < P->nreact; r++) {
+                                double kr = P->A[r];
+                                if (P->Ea[r] != 0.0) kr = P->A[r] * std::exp(-P->Ea[r] / (RU * temp));
+                                for (int q = 0; q < ns; q++) {
+                                    if (!(P->order[r][q] > 0.0)) continue;
+                                    double dr = kr;
+                                    for (int p = 0; p < ns; p++) {
+                                        const double o = P->order[r][p];
+                                        if (!(o > 0.0)) continue;
+                                        dr *= (p == q) ? o * std::pow(y[p], o - 1.0) : std::pow(y[p], o);
+                                    }
+                                    for (int s = 0; s < ns; s++)
+                                        if (std::fabs(P->nu[r][s]) > 0.0) W[s][q] += P->nu[r][s] * dr;
+                                }
+                            }
+                        for (int s = 0; s < ns; s++) {
+                            for (int q = 0; q < ns; q++) W[s][q] = -(g * h) * W[s][q];
+                            W[s][s] += 1.0;
+                        }
+                        // LU with partial pivoting
+                        for (int kk = 0; kk < ns; kk++) {
+                            int p = kk;
+                            for (int ii = kk + 1; ii < ns; ii++)
+                                if (std::fabs(W[ii][kk]) > std::fabs(W[p][kk])) p = ii;
+                            piv[kk] = p;
+                            if (p != kk)
+                                for (int jj = 0; jj < ns; jj++) std::swap(W[kk][jj], W[p][jj]);
+                            for (int ii = kk + 1; ii < ns; ii++) {
+                                W[ii][kk] /= W[kk][kk];
+                                for (int jj = kk + 1; jj < ns; jj++) W[ii][jj] -= W[ii][kk] * W[kk][jj];
+                            }
+                        }
+                        auto solve = [&](double* x) {
+                            for (int kk = 0; kk < ns; kk++)
+                                if (piv[kk] != kk) std::swap(x[kk], x[piv[kk]]);
+                            for (int ii = 1; ii < ns; ii++)
+                                for (int jj = 0; jj < ii; jj++) x[ii] -= W[ii][jj] * x[jj];
+                            for (int ii = ns - 1; ii >= 0; ii--) {
+                                for (int jj = ii + 1; jj < ns; jj++) x[ii] -= W[ii][jj] * x[jj];
+                                x[ii] /= W[ii][ii];
+                            }
+                        };
+                        for (int s = 0; s < ns; s++) k1[s] = f0[s];
+                        solve(k1);
+                        for (int s = 0; s < ns; s++) y1[s] = y[s] + h * k1[s];
+                        compute_spec_source(c, y1, temp, k2);
+                        for (int s = 0; s < ns; s++) k2[s] -= 2.0 * k1[s];
+                        solve(k2);
+                        double e2 = 0.0;
+                        for (int s = 0; s < ns; s++) {
+                            const double yn = y[s] + (1.5 * h) * k1[s] + (0.5 * h) * k2[s];
+                            const double err = (0.5 * h) * (k1[s] + k2[s]);
+                            const double sc = atol + rtol * std::max(std::fabs(y[s]), std::fabs(yn));
+                            e2 += (err / sc) * (err / sc);
+                            y1[s] = yn;
+                        }
+                        const double en = std::sqrt(e2 / ns);
+                        if (en <= 1.0) {
+                            for (int s = 0; s < ns; s++) y[s] = y1[s];
+                            t += h;
+                            if (last) done = true;
+                        }
+                        h *= (en > 0.0) ? std::min(5.0, std::max(0.2, 0.9 / std::sqrt(en))) : 5.0;
+                    }
+                    if (!done) status = MFG_ERR_TIMEOUT;
+                    for (int s = 0; s < ns; s++) sn(i, j, k, FLO_NVARS + s) = y[s];
+                }
+    }
+    return status;
+}
+
 // mflo::Advance_chemistry (Source/mflo_splitchem.cpp:177-199), after its
 // swap: the stage-1 source on the incoming s_old, the midpoint
 // 1*X + (half dt) F in the s_new buffer, the stage-2 source there, then

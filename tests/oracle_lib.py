@@ -35,6 +35,7 @@ def load(variant="strict"):
         "oracle_advance": [PP, GP, BP, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_double)],
         "oracle_advance_amr": [PP, GP, BP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int],
         "oracle_chem_advance_rk2": [PP, BP, C.c_int, C.c_double],
+        "oracle_chem_substep_ros2": [PP, BP, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int],
         "oracle_store_inertgas_conc": [PP, BP, C.c_int],
         "oracle_update_vars_after_chemsolve": [PP, BP, C.c_int, C.c_int],
         "oracle_abi_layout": [C.POINTER(C.c_int64), C.c_int],

@@ -137,3 +137,40 @@ def test_oracle_two_level_step_conserves_composite_totals():
     crse = o.box_state(0)  # coarse box 0 holds coarse cells 0..5 in each direction
     # (conserved components: the primitive refresh after the step recomputes the others)
     assert np.allclose(crse[comps, 2:6, 2:6, 2:6], avg[comps, 0:4, 0:4, 0:4], rtol=1e-14, atol=0)
+
+
+def _stiff_decay_case(k=1e10):
+    """Catalyst layout with one reaction A -> B, first order in A, rate k."""
+    c = cases.catalyst(n=8, order=5, max_grid=8)
+    P = c.params
+    P.nreact = 1
+    for s in range(abi.MAX_SPECIES):
+        P.nu[0][s] = 0.0
+        P.order[0][s] = 0.0
+    P.nu[0][0], P.nu[0][1], P.order[0][0] = -1.0, 1.0, 1.0
+    P.A[0], P.Ea[0] = k, 0.0
+    return c
+
+
+def test_oracle_ros2_stiff_decay():
+    """The implicit (ROS2) chemistry of the oracle on A -> B with k dt = 1e4
+    (explicit RK3 is unstable beyond k dt ~ 2.5): A decays to nothing (the
+    method is L-stable), A + B is conserved to rounding (Rosenbrock stages
+    keep linear invariants), and the adaptive steps resolve the transient."""
+    c = _stiff_decay_case()
+    o = OracleLevel(c)
+    lev = o.level
+    lev.s_old[0][...] = lev.s_new[0]
+    a0, b0 = lev.s_new[0][abi.FLO_NVARS].copy(), lev.s_new[0][abi.FLO_NVARS + 1].copy()
+    rc = o.lib.oracle_chem_substep_ros2(C.byref(c.params), o.desc, 1, 1e-6, 1e-3, 1e-6, 2000)
+    assert rc == 0
+    a1, b1 = lev.s_new[0][abi.FLO_NVARS], lev.s_new[0][abi.FLO_NVARS + 1]
+    assert np.all(np.abs(a1) <= 1e-6 * a0.max())
+    assert np.allclose(a1 + b1, a0 + b0, rtol=1e-13, atol=0)
+    # at k dt = 0.5 the result matches exp(-k dt) to the tolerance
+    c = _stiff_decay_case(k=5e5)
+    o = OracleLevel(c)
+    o.level.s_old[0][...] = o.level.s_new[0]
+    a0 = o.level.s_new[0][abi.FLO_NVARS].copy()
+    assert o.lib.oracle_chem_substep_ros2(C.byref(c.params), o.desc, 1, 1e-6, 1e-6, 1e-12, 2000) == 0
+    assert np.allclose(o.level.s_new[0][abi.FLO_NVARS], a0 * np.exp(-0.5), rtol=2e-5, atol=0)
