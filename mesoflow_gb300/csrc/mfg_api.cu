@@ -208,6 +208,7 @@ int mfg_init(const mfg_params* p) {
     for (int s = 0; s <= p->ngas && s <= MFG_MAX_SPECIES; ++s) {
         if (s == p->ngas && p->thermo_kind != MFG_THERMO_BG_GAS) break;
         h.cv[s] = R / (p->gamma[s] - 1.0);
+        h.igm1[s] = 1.0 / (p->gamma[s] - 1.0);
         if (s < p->ngas && p->molwt[s] != 0.0) h.cvmass[s] = R / (p->gamma[s] - 1.0) / p->molwt[s];
     }
     auto hmean = [](double d1, double d2) { return 2.0 * d1 * d2 / (d1 + d2 + 1e-30); };

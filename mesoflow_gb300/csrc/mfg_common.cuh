@@ -32,6 +32,7 @@ struct DevParams {
     double molwt[MAXS];
     double gamma[MAXS + 1];
     double cv[MAXS + 1];       // R/(gamma_k - 1) per gas species (+ background gas)
+    double igm1[MAXS + 1];     // 1/(gamma_k - 1)
     double cvmass[MAXS];       // R/(gamma_k - 1)/W_k (mass-cv energy form)
     double advect_flag[MAXS];
     int visc_mode, cond_mode;

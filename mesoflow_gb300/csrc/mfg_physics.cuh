@@ -120,18 +120,22 @@ __device__ __forceinline__ double thermo_gamma(double rho, const double* spec) {
         for (int s = 0; s < NS; ++s)
             if (s < P.ngas) sum_ci += spec[s];
         sum_ci += c_bg;
+        const double isum = 1.0 / sum_ci;
 #pragma unroll
         for (int s = 0; s < NS; ++s)
-            if (s < P.ngas) term2 += (spec[s] / sum_ci) / (P.gamma[s] - 1.0);
-        term2 += (c_bg / sum_ci) / (P.gamma[P.ngas] - 1.0);
+            if (s < P.ngas) term2 += (spec[s] * isum) * P.igm1[s];
+        term2 += (c_bg * isum) * P.igm1[P.ngas];
         return 1.0 + 1.0 / term2;
     }
 #pragma unroll
     for (int s = 0; s < NS; ++s)
         if (s < P.ngas) sum_ci += spec[s];
+    // mole fractions x_s = c_s / sum c and 1/(gamma_s - 1) as products: one
+    // division instead of two per species
+    const double isum = 1.0 / sum_ci;
 #pragma unroll
     for (int s = 0; s < NS; ++s)
-        if (s < P.ngas) term2 += (spec[s] / sum_ci) / (P.gamma[s] - 1.0);
+        if (s < P.ngas) term2 += (spec[s] * isum) * P.igm1[s];
     return 1.0 + 1.0 / term2;
 }
 

@@ -35,6 +35,40 @@ __device__ __forceinline__ void cell_of(const Valid& v, int64_t t, int& i, int& 
 // py_utils/rxnscheme_writer/example/chemistry.H:27-54).  Rate constant:
 // A_r, or A_r exp(-Ea_r/(RU T)) when Ea_r != 0.  Integer reaction orders 1
 // and 2 are exact products (pow(c,1) = c, pow(c,2) = c*c).
+// Rate constants of every reaction at temperature temp.
+__device__ __forceinline__ void rate_constants(double temp, double* kr) {
+    const DevParams& P = c_P;
+    for (int r = 0; r < P.nreact; ++r) {
+        kr[r] = P.A[r];
+        if (P.Ea[r] != 0.0) kr[r] = P.A[r] * exp(-P.Ea[r] / (kRU * temp));
+    }
+}
+
+// wdot from precomputed rate constants (the chemistry sub-steps hold the
+// temperature fixed, so their stages share one set).
+template <int NS>
+__device__ __forceinline__ void spec_source_k(const double* spec, const double* kr, double* wdot) {
+    const DevParams& P = c_P;
+#pragma unroll
+    for (int s = 0; s < NS; ++s) wdot[s] = 0.0;
+    if (!P.chem_on) return;
+    for (int r = 0; r < P.nreact; ++r) {
+        double cm = 1.0;
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            const double o = P.order[r][s];
+            if ((P.ord_mask[r] >> s) & 1u) {
+                const double c = spec[s];
+                cm *= (o == 1.0) ? c : (o == 2.0) ? c * c : pow(c, o);
+            }
+        }
+        const double rate = kr[r] * cm;
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if ((P.nu_mask[r] >> s) & 1u) wdot[s] += P.nu[r][s] * rate;
+    }
+}
+
 template <int NS>
 __device__ __forceinline__ void spec_source(const double* spec, double temp, double* wdot) {
     const DevParams& P = c_P;
@@ -240,15 +274,17 @@ __device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So,
 #pragma unroll
     for (int s = 0; s < NS; ++s) s0[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
     const double temp = So(i, j, k, TEMP);
-    spec_source<NS>(s0, temp, f0);
+    double kr[MAXR];
+    rate_constants(temp, kr);
+    spec_source_k<NS>(s0, kr, f0);
     const double c10 = dt * 1.0, c20 = dt * 0.25, c21 = dt * 0.25;
 #pragma unroll
     for (int s = 0; s < NS; ++s) s1[s] = add(s0[s], mul(c10, add(0.0, add(0.0, f0[s]))));
-    spec_source<NS>(s1, temp, f1);
+    spec_source_k<NS>(s1, kr, f1);
 #pragma unroll
     for (int s = 0; s < NS; ++s)
         s1[s] = add(add(s0[s], mul(c20, add(0.0, add(0.0, f0[s])))), mul(c21, add(0.0, add(0.0, f1[s]))));
-    spec_source<NS>(s1, temp, f2);
+    spec_source_k<NS>(s1, kr, f2);
     const double w0 = dt * (1.0 / 6.0), w1 = dt * (1.0 / 6.0), w2 = dt * (2.0 / 3.0);
     for (int n = 0; n < ncomp; ++n) {
         if (n >= NFLO) continue;
