@@ -386,6 +386,15 @@ int mfg_boxlist_step(mfg_boxlist* list, double time, double dt, int mode, void* 
 int mfg_boxlist_evolve(mfg_boxlist* list, double final_time, double stop_time, int max_step, double* time,
                        double* dt, int* istep, void* stream);
 
+/* The same device-resident loop for the subcycled hierarchy (mfg_boxlist_step_amr
+ * steps): ComputeDt with subcycling on the device (per level EstTimeStep x cfl
+ * capped at 1.1 x the level's previous dt, dt0 = min over levels of the ratio
+ * product x that, stop-time clamp, dt_l = dt_{l-1} / ratio_l), the fill
+ * coefficients of the coarse step computed on the device, then the step.
+ * dt holds nlev doubles: each level's previous dt (1e100 before the first). */
+int mfg_boxlist_evolve_amr(mfg_boxlist* list, double final_time, double stop_time, int max_step, double* time,
+                           double* dt, int* istep, void* stream);
+
 /* One coarse step of the reference's multi-level time stepping over the whole
  * hierarchy (mflo::EvolveAMR's step, Source/mflo_evolve.cpp:26-58, and
  * mflo::timeStep, :174-247): level l advances with dt0 / (ratio_1 ... ratio_l)

@@ -112,6 +112,8 @@ SIGNATURES = [
     ("mfg_boxlist_step_amr", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),
     ("mfg_boxlist_evolve", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int), _VP]),
+    ("mfg_boxlist_evolve_amr", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_int), _VP]),
     ("mfg_chem_advance_rk2", C.c_int, [_BP, C.c_int, C.c_double, C.c_double, _VP]),
     ("mfg_set_chem_integrator", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_int]),
     ("mfg_store_inertgas_conc", C.c_int, [_BP, C.c_int, _VP]),

@@ -19,6 +19,7 @@
 // which launches per box (RHS, cut cells, bookends) and per level (fill).
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -81,6 +82,8 @@ struct RunState {
     double final_time, stop_time, cfl;
     int istep, max_step, nlev;
     double acc[2 * RUN_MAXLEV];  // per level: max wave speed, max species diffusivity
+    // subcycled loop: per-level dt of this step and of the previous one
+    double dtl[RUN_MAXLEV], dtl_prev[RUN_MAXLEV];
 };
 
 enum Phase { PH_GROWN = 0, PH_VALID, PH_FACE, PH_FLUX, PH_UPDATE, PH_COUNT };
@@ -394,15 +397,25 @@ __global__ void __launch_bounds__(BT) bk_cp_bc(const MBox* __restrict__ boxes, c
 // Flux registers (AMReX FluxRegister).  One thread per (register cell, advected
 // component c); registers are stored component-major, reg[c * ne + e].
 // CrseInit(ADD): reg += F_coarse * scale_d
+// With dtp (device dt of the level), scale_d = ((sgn dt) dA_d) w instead of s_d.
+struct RegScale {
+    double s[3];       // scales for a host dt
+    double dA[3], w;   // face areas and stage weight, for a device dt
+    double sgn;        // -1 CrseInit, +1 FineAdd
+};
+__device__ __forceinline__ double reg_scale(const RegScale& S, const double* dtp, int d) {
+    return dtp ? __dmul_rn(__dmul_rn(S.sgn * (*dtp), S.dA[d]), S.w) : S.s[d];
+}
+
 __global__ void __launch_bounds__(BT) bk_reg_crse(const RegEnt* __restrict__ ent, int ne,
                                                   const RhsBox* __restrict__ rhs, double* __restrict__ reg,
-                                                  double s0, double s1, double s2) {
+                                                  RegScale S, const double* __restrict__ dtp) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     const int c = blockIdx.y;
     const RegEnt E = ent[e];
     const Fab& F = rhs[E.cb].flx[E.d];
-    const double scale = E.d == 0 ? s0 : E.d == 1 ? s1 : s2;
+    const double scale = reg_scale(S, dtp, E.d);
     double& r = reg[(size_t)c * ne + e];
     r = __dadd_rn(r, __dmul_rn(F.p[F.off(E.cf[0], E.cf[1], E.cf[2]) + c * F.ns], scale));
 }
@@ -411,13 +424,13 @@ __global__ void __launch_bounds__(BT) bk_reg_crse(const RegEnt* __restrict__ ent
 // transverse direction outer
 __global__ void __launch_bounds__(BT) bk_reg_fine(const RegEnt* __restrict__ ent, int ne,
                                                   const RhsBox* __restrict__ rhs, double* __restrict__ reg,
-                                                  double s0, double s1, double s2, int ratio) {
+                                                  RegScale S, const double* __restrict__ dtp, int ratio) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     const int c = blockIdx.y;
     const RegEnt E = ent[e];
     const Fab& F = rhs[E.fb].flx[E.d];
-    const double scale = E.d == 0 ? s0 : E.d == 1 ? s1 : s2;
+    const double scale = reg_scale(S, dtp, E.d);
     const int t1 = E.d == 0 ? 1 : 0, t2 = E.d == 2 ? 1 : 2;
     const int64_t st[3] = {1, F.js, F.ks};
     const int64_t q = F.off(E.ff[0], E.ff[1], E.ff[2]) + c * F.ns;
@@ -680,6 +693,98 @@ __global__ void bk_run_advance(RunState* __restrict__ R, cudaGraphConditionalHan
     cudaGraphSetConditional(h, c);
 }
 
+// ComputeDt of the subcycled hierarchy (Source/mflo_timestep.cpp:18-50):
+// per level EstTimeStep x cfl capped at 1.1 x the level's previous dt,
+// dt_0 = min over levels of (product of ratios up to l) x that, the stop-time
+// clamp, then dt_l = dt_{l-1} / ratio_l.
+__global__ void bk_compute_dt_amr(const LevelG* __restrict__ lev, RunState* __restrict__ R) {
+    double tmp[RUN_MAXLEV];
+    for (int l = 0; l < R->nlev; ++l) {
+        const double h0 = R->acc[2 * l], h1 = R->acc[2 * l + 1];
+        double est = 1.7976931348623157e308;
+        if (h0 > 0)
+            for (int d = 0; d < 3; ++d) est = dmin_(est, __ddiv_rn(lev[l].dx[d], h0));
+        if (h1 > 0)
+            for (int d = 0; d < 3; ++d)
+                est = dmin_(est, __ddiv_rn(__ddiv_rn(__dmul_rn(__dmul_rn(0.5, lev[l].dx[d]), lev[l].dx[d]), h1), 3.0));
+        tmp[l] = __dmul_rn(est, R->cfl);
+    }
+    double dt0 = tmp[0];
+    int nf = 1;
+    for (int l = 0; l < R->nlev; ++l) {
+        tmp[l] = dmin_(tmp[l], __dmul_rn(1.1, R->dtl_prev[l]));
+        nf *= (l > 0) ? lev[l].ratio : 1;
+        dt0 = dmin_(dt0, __dmul_rn((double)nf, tmp[l]));
+    }
+    const double eps = __dmul_rn(1e-3, dt0);
+    if (__dadd_rn(R->t, dt0) > __dsub_rn(R->stop_time, eps)) dt0 = __dsub_rn(R->stop_time, R->t);
+    R->dtl[0] = dt0;
+    for (int l = 1; l < R->nlev; ++l) R->dtl[l] = __ddiv_rn(R->dtl[l - 1], (double)lev[l].ratio);
+}
+
+// The coarse-data coefficients of every fill of one coarse step, in the order
+// of the host recursion (amr_time_step): level l advancing from `time` sets
+// t_old = t_new, t_new += dt_l, and its three stages read level l-1 at time,
+// time + dt_l, time + dt_l (mflo::GetData); the substeps of level l+1 start at
+// time + (i-1) dt_{l+1}.
+__global__ void bk_amr_plan(const LevelG* __restrict__ lev, const RunState* __restrict__ R,
+                            TCoef* __restrict__ coef) {
+    const int nlev = R->nlev;
+    double t_old[RUN_MAXLEV], t_new[RUN_MAXLEV], ftime[RUN_MAXLEV];
+    int fnext[RUN_MAXLEV];
+    for (int l = 0; l < nlev; ++l) t_old[l] = t_new[l] = R->t;
+    int ev = 0;
+    // level 0: no coarser data
+    t_old[0] = t_new[0];
+    t_new[0] = __dadd_rn(t_new[0], R->dtl[0]);
+    ftime[0] = R->t;
+    fnext[0] = 1;
+    int depth = 0;
+    while (depth >= 0) {
+        const int lc = depth;
+        if (lc + 1 < nlev && fnext[lc] <= lev[lc + 1].ratio) {
+            const int i = fnext[lc]++;
+            const int lf = lc + 1;
+            const double dtf = R->dtl[lf];
+            const double time = __fma_rn((double)(i - 1), dtf, ftime[lc]);
+            t_old[lf] = t_new[lf];
+            t_new[lf] = __dadd_rn(t_new[lf], dtf);
+            for (int stage = 1; stage <= 3; ++stage) {
+                const double T = stage == 1 ? time : __dadd_rn(time, dtf);
+                const int l = lf - 1;
+                TCoef c{0, 0.0, 0.0};
+                const double teps = __dmul_rn(__dsub_rn(t_new[l], t_old[l]), 1.e-3);
+                if (T > __dsub_rn(t_new[l], teps) && T < __dadd_rn(t_new[l], teps)) {
+                    c.kind = 1;
+                } else if (T > __dsub_rn(t_old[l], teps) && T < __dadd_rn(t_old[l], teps)) {
+                    c.kind = 0;
+                } else {
+                    c.kind = 2;
+                    c.a = __ddiv_rn(__dsub_rn(t_new[l], T), __dsub_rn(t_new[l], t_old[l]));
+                    c.b = __ddiv_rn(__dsub_rn(T, t_old[l]), __dsub_rn(t_new[l], t_old[l]));
+                }
+                coef[ev++] = c;
+            }
+            ftime[lf] = time;
+            fnext[lf] = 1;
+            depth = lf;
+        } else {
+            --depth;
+        }
+    }
+}
+
+__global__ void bk_run_advance_amr(RunState* __restrict__ R, cudaGraphConditionalHandle h) {
+    const double dt = R->dtl[0];
+    R->t = __dadd_rn(R->t, dt);
+    R->istep += 1;
+    for (int l = 0; l < R->nlev; ++l) R->dtl_prev[l] = R->dtl[l];
+    for (int q = 0; q < 2 * RUN_MAXLEV; ++q) R->acc[q] = 0.0;
+    unsigned c = run_continue(R);
+    if (R->t >= __dsub_rn(R->stop_time, __dmul_rn(1e-6, dt))) c = 0u;
+    cudaGraphSetConditional(h, c);
+}
+
 #undef TILE_LOOP
 #undef TILE_END
 
@@ -746,6 +851,7 @@ struct mfg_boxlist {
     // device-resident time loop (mfg_boxlist_evolve)
     RunState* d_run = nullptr;
     cudaGraphExec_t gexec_run = nullptr;
+    cudaGraphExec_t gexec_run_amr = nullptr;
 };
 
 namespace {
@@ -970,6 +1076,8 @@ void drop_graph(mfg_boxlist& L) {
     L.gexec_amr = nullptr;
     if (L.gexec_run) cudaGraphExecDestroy(L.gexec_run);
     L.gexec_run = nullptr;
+    if (L.gexec_run_amr) cudaGraphExecDestroy(L.gexec_run_amr);
+    L.gexec_run_amr = nullptr;
 }
 
 // ---- multi-level step -------------------------------------------------------------
@@ -1202,6 +1310,7 @@ struct AmrRun {
     int mode = 1;
     cudaStream_t st = nullptr;
     int rc = MFG_OK;
+    const double* ddt = nullptr;  // device per-level dt (mfg_boxlist_evolve_amr), batched mode only
 };
 
 // Coarse data of level l at time T (mflo::GetData, Source/mflo.cpp:310-330):
@@ -1277,7 +1386,7 @@ void amr_stage(mfg_boxlist& L, AmrRun& R, int l, int stage, double dtl) {
         const TSet T = level_tiles(L, l);
         if (T[PH_VALID].n) {
             b_cutcells(L, T[PH_VALID], st);
-            b_rhs(L, T, stage, dtl, st);
+            b_rhs(L, T, stage, dtl, st, R.ddt ? R.ddt + l : nullptr);
         }
     }
     // flux registers
@@ -1285,16 +1394,18 @@ void amr_stage(mfg_boxlist& L, AmrRun& R, int l, int stage, double dtl) {
     const double ff = stage < 3 ? kSixth : kTwo3rd;
     const double* dx = L.geoms[l].dx;
     const double dA[3] = {dx[1] * dx[2], dx[0] * dx[2], dx[0] * dx[1]};
+    const double* dtp = R.ddt ? R.ddt + l : nullptr;
     ProfScope ps(K_AMR_SYNC, st);
     if (l + 1 < L.nlev && L.nent[l + 1]) {
         const int ne = L.nent[l + 1];
-        bk_reg_crse<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l + 1], ne, L.d_rhs, L.d_reg[l + 1],
-                                                               -dtl * dA[0] * ff, -dtl * dA[1] * ff, -dtl * dA[2] * ff);
+        const RegScale S = {{-dtl * dA[0] * ff, -dtl * dA[1] * ff, -dtl * dA[2] * ff}, {dA[0], dA[1], dA[2]}, ff, -1.0};
+        bk_reg_crse<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l + 1], ne, L.d_rhs, L.d_reg[l + 1], S, dtp);
     }
     if (l > 0 && L.nent[l]) {
         const int ne = L.nent[l];
-        bk_reg_fine<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l], ne, L.d_rhs, L.d_reg[l], dtl * dA[0] * ff,
-                                                               dtl * dA[1] * ff, dtl * dA[2] * ff, L.levg[l].ratio);
+        const RegScale S = {{dtl * dA[0] * ff, dtl * dA[1] * ff, dtl * dA[2] * ff}, {dA[0], dA[1], dA[2]}, ff, 1.0};
+        bk_reg_fine<<<dim3((ne + BT - 1) / BT, C), BT, 0, st>>>(L.d_ent[l], ne, L.d_rhs, L.d_reg[l], S, dtp,
+                                                               L.levg[l].ratio);
     }
 }
 
@@ -1308,7 +1419,7 @@ void amr_chem(mfg_boxlist& L, AmrRun& R, int l, double dtl) {
     const PhaseTiles& V = level_tiles(L, l)[PH_VALID];
     if (!V.n) return;
     ProfScope ps(K_CHEM, R.st);
-    NS_DISPATCH(bk_chem, (V.grid, BT, 0, R.st), (L.d_mbox, V.d, V.n, dtl, nc, (const double*)nullptr));
+    NS_DISPATCH(bk_chem, (V.grid, BT, 0, R.st), (L.d_mbox, V.d, V.n, dtl, nc, R.ddt ? R.ddt + l : nullptr));
 }
 
 void amr_sync(mfg_boxlist& L, AmrRun& R, int l) {  // reflux of level l, average_down of l+1 onto l
@@ -1351,16 +1462,20 @@ void amr_advance(mfg_boxlist& L, AmrRun& R, int l, double time, double dtl) {
 void amr_time_step(mfg_boxlist& L, AmrRun& R, int l, double time) {
     amr_advance(L, R, l, time, R.dt[l]);
     if (l + 1 < L.nlev) {
-        for (int i = 1; i <= L.levg[l + 1].ratio; ++i) amr_time_step(L, R, l + 1, time + (i - 1) * R.dt[l + 1]);
+        // time + (i-1) dt_{l+1} as one rounding, as the device plan computes it
+        for (int i = 1; i <= L.levg[l + 1].ratio; ++i)
+            amr_time_step(L, R, l + 1, std::fma((double)(i - 1), R.dt[l + 1], time));
         if (R.launch) amr_sync(L, R, l);
     }
 }
 
-int amr_run(mfg_boxlist& L, double time, double dt0, bool launch, int mode, cudaStream_t st) {
+int amr_run(mfg_boxlist& L, double time, double dt0, bool launch, int mode, cudaStream_t st,
+            const double* ddt = nullptr) {
     AmrRun R;
     R.launch = launch;
     R.mode = mode;
     R.st = st;
+    R.ddt = ddt;
     R.t_old.assign(L.nlev, time);
     R.t_new.assign(L.nlev, time);
     R.dt.assign(L.nlev, dt0);
@@ -1379,6 +1494,63 @@ int amr_run(mfg_boxlist& L, double time, double dt0, bool launch, int mode, cuda
     }
     amr_note(R, cudaGetLastError());
     return R.rc;
+}
+
+// The device time loop as one graph: an init kernel setting the loop
+// condition, then a WHILE node whose body is one step with its ComputeDt
+// (common dt, or the subcycled hierarchy with the fill plan) and the kernel
+// that advances the time and sets the condition again.
+bool build_run_graph(mfg_boxlist& L, cudaStream_t st, bool amr) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t n0, wn;
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof(kp));
+    RunState* R = L.d_run;
+    void* args[] = {&R, &h};
+    kp.func = (void*)bk_run_init;
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = args;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    bool ok = cudaGraphConditionalHandleCreate(&h, g, 0, 0) == cudaSuccess &&
+              cudaGraphAddKernelNode(&n0, g, nullptr, 0, &kp) == cudaSuccess;
+    if (ok) {
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        ok = cudaGraphAddNode(&wn, g, &n0, nullptr, 1, &cp) == cudaSuccess;
+    }
+    if (ok) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            const PhaseTiles& V = L.ph[PH_VALID];
+            NS_DISPATCH(bk_timestep, (V.grid, BT, 0, st), (L.d_mbox, V.d, V.n, R));
+            if (amr) {
+                bk_compute_dt_amr<<<1, 1, 0, st>>>(L.d_lev, R);
+                bk_amr_plan<<<1, 1, 0, st>>>(L.d_lev, R, L.d_coef);
+                const int rc = amr_run(L, 0.0, 0.0, true, 1, st, R->dtl);
+                ok = rc == MFG_OK;
+                bk_run_advance_amr<<<1, 1, 0, st>>>(R, h);
+            } else {
+                bk_compute_dt<<<1, 1, 0, st>>>(L.d_lev, R);
+                step_batched(L, 0.0, st, &R->dt);
+                bk_run_advance<<<1, 1, 0, st>>>(R, h);
+            }
+            ok = (cudaStreamEndCapture(st, &body) == cudaSuccess) && ok;
+        }
+    }
+    cudaGraphExec_t& ex = amr ? L.gexec_run_amr : L.gexec_run;
+    if (ok) ok = cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        ex = nullptr;
+        note_cuda_error(cudaGetLastError(), "building the device time loop");
+    }
+    return ok;
 }
 
 int sm_count() {
@@ -1614,49 +1786,7 @@ int mfg_boxlist_evolve(mfg_boxlist* L, double final_time, double stop_time, int 
             return MFG_ERR_CUDA;
     }
     if (!L->d_run && cudaMalloc(&L->d_run, sizeof(RunState)) != cudaSuccess) return MFG_ERR_CUDA;
-    if (!L->gexec_run) {
-        cudaGraph_t g = nullptr;
-        if (cudaGraphCreate(&g, 0) != cudaSuccess) return MFG_ERR_CUDA;
-        cudaGraphConditionalHandle h;
-        cudaGraphNode_t n0, wn;
-        cudaKernelNodeParams kp;
-        memset(&kp, 0, sizeof(kp));
-        RunState* R = L->d_run;
-        void* args[] = {&R, &h};
-        kp.func = (void*)bk_run_init;
-        kp.gridDim = dim3(1);
-        kp.blockDim = dim3(1);
-        kp.kernelParams = args;
-        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-        bool ok = cudaGraphConditionalHandleCreate(&h, g, 0, 0) == cudaSuccess &&
-                  cudaGraphAddKernelNode(&n0, g, nullptr, 0, &kp) == cudaSuccess;
-        if (ok) {
-            cp.conditional.handle = h;
-            cp.conditional.type = cudaGraphCondTypeWhile;
-            cp.conditional.size = 1;
-            ok = cudaGraphAddNode(&wn, g, &n0, nullptr, 1, &cp) == cudaSuccess;
-        }
-        if (ok) {
-            cudaGraph_t body = cp.conditional.phGraph_out[0];
-            ok = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
-                 cudaSuccess;
-            if (ok) {
-                const PhaseTiles& V = L->ph[PH_VALID];
-                NS_DISPATCH(bk_timestep, (V.grid, BT, 0, st), (L->d_mbox, V.d, V.n, R));
-                bk_compute_dt<<<1, 1, 0, st>>>(L->d_lev, R);
-                step_batched(*L, 0.0, st, &R->dt);
-                bk_run_advance<<<1, 1, 0, st>>>(R, h);
-                ok = cudaStreamEndCapture(st, &body) == cudaSuccess;
-            }
-        }
-        if (ok) ok = cudaGraphInstantiate(&L->gexec_run, g, 0) == cudaSuccess;
-        cudaGraphDestroy(g);
-        if (!ok) {
-            L->gexec_run = nullptr;
-            note_cuda_error(cudaGetLastError(), "building the device time loop");
-            return MFG_ERR_CUDA;
-        }
-    }
+    if (!L->gexec_run && !build_run_graph(*L, st, false)) return MFG_ERR_CUDA;
     RunState hs;
     memset(&hs, 0, sizeof(hs));
     hs.t = *time;
@@ -1673,6 +1803,49 @@ int mfg_boxlist_evolve(mfg_boxlist* L, double final_time, double stop_time, int 
     if (cudaStreamSynchronize(st) != cudaSuccess) return MFG_ERR_CUDA;
     *time = hs.t;
     *dt = hs.dt_prev;
+    *istep = hs.istep;
+    unsigned v = 0;
+    if (read_status(&v, false) != cudaSuccess) return MFG_ERR_CUDA;
+    if (v & MFG_STATUS_NAN) return MFG_ERR_NAN;
+    if (v & MFG_STATUS_NEG_PRESSURE) return MFG_ERR_NEG_PRESSURE;
+    return MFG_OK;
+}
+
+// mflo::EvolveAMR's loop for the subcycled hierarchy, on the device.
+int mfg_boxlist_evolve_amr(mfg_boxlist* L, double final_time, double stop_time, int max_step, double* time,
+                           double* dt, int* istep, void* stream) {
+    if (!L || !time || !dt || !istep || !stream) return MFG_ERR_ARG;
+    if (L->amr_rc) return L->amr_rc;
+    if (L->nlev > RUN_MAXLEV) return MFG_ERR_ARG;
+    if (profile_enabled()) return MFG_ERR_STATE;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (L->flux_tiles_kind != flux_kind(*L)) {
+        drop_graph(*L);
+        if (build_tiles(*L, L->ph[PH_FLUX], PH_FLUX, L->ph[PH_FLUX].tile_items, -1) != cudaSuccess)
+            return MFG_ERR_CUDA;
+    }
+    if (L->lt_version != L->tile_version || L->lt_flux_kind != flux_kind(*L)) {
+        drop_graph(*L);
+        if (build_level_tiles(*L) != cudaSuccess) return MFG_ERR_CUDA;
+    }
+    if (!L->d_run && cudaMalloc(&L->d_run, sizeof(RunState)) != cudaSuccess) return MFG_ERR_CUDA;
+    if (!L->gexec_run_amr && !build_run_graph(*L, st, true)) return MFG_ERR_CUDA;
+    RunState hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.t = *time;
+    hs.final_time = final_time;
+    hs.stop_time = stop_time;
+    hs.cfl = c_host_params().cfl;
+    hs.istep = *istep;
+    hs.max_step = max_step;
+    hs.nlev = L->nlev;
+    for (int l = 0; l < L->nlev; ++l) hs.dtl_prev[l] = dt[l];
+    if (cudaMemcpyAsync(L->d_run, &hs, sizeof(hs), cudaMemcpyHostToDevice, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaGraphLaunch(L->gexec_run_amr, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaMemcpyAsync(&hs, L->d_run, sizeof(hs), cudaMemcpyDeviceToHost, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MFG_ERR_CUDA;
+    *time = hs.t;
+    for (int l = 0; l < L->nlev; ++l) dt[l] = hs.dtl_prev[l];
     *istep = hs.istep;
     unsigned v = 0;
     if (read_status(&v, false) != cudaSuccess) return MFG_ERR_CUDA;

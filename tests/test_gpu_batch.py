@@ -253,3 +253,65 @@ def test_device_time_loop_equals_host_loop(name):
     assert nn.value == n and tt.value == t and dd.value == dtp, (nn.value, n, tt.value, t)
     assert n >= 5
     assert np.array_equal(a.get_state(c.shape_zyx), b.get_state(c.shape_zyx))
+
+
+def test_device_amr_loop_equals_host_loop():
+    """mfg_boxlist_evolve_amr (subcycled ComputeDt and the coarse step's fill
+    coefficients on the device, one graph launch) gives bitwise the states,
+    time, per-level dt and step count of the host loop of per-level
+    mfg_est_timestep, ComputeDt with subcycling (Source/mflo_timestep.cpp:18-50)
+    and mfg_boxlist_step_amr, including a last step clamped to the stop time."""
+    amr = cases.catalyst_amr(n0=32, nlev=3, order=5, blocking=8, max_grid=16, base_grid=16, nspheres=6)
+    lib = abi.load()
+    abi.check("mfg_init", lib.mfg_init(C.byref(amr.params)))
+    s = torch.cuda.Stream()
+    st = C.c_void_p(s.cuda_stream)
+    nlev = len(amr.geoms)
+    ratio = [1] + [int(round(amr.geoms[l - 1].dx[0] / amr.geoms[l].dx[0])) for l in range(1, nlev)]
+    ma, mb = MultiLevel(amr, backend="torch", device="cuda"), MultiLevel(amr, backend="torch", device="cuda")
+    ha = _boxlist(lib, ma.descriptors(), len(amr.boxes), ma.geoms(), nlev)
+    hb = _boxlist(lib, mb.descriptors(), len(amr.boxes), mb.geoms(), nlev)
+    est = C.c_double()
+
+    def est_levels():
+        out = []
+        for l in range(nlev):
+            lv = ma.levels[l]
+            abi.check("est", lib.mfg_est_timestep(lv.descriptors(), len(lv.s_new), C.byref(amr.geoms[l]), 0.0,
+                                                  C.byref(est), st))
+            out.append(est.value)
+        return out
+
+    with torch.cuda.stream(s):
+        stop = 2.5 * 4 * est_levels()[-1]
+        t, n, dtp = 0.0, 0, [1e100] * nlev
+        while n < 6 and t < stop:
+            tmp = est_levels()
+            dt0, nf = tmp[0], 1
+            for l in range(nlev):
+                tmp[l] = min(tmp[l], 1.1 * dtp[l])
+                nf *= ratio[l]
+                dt0 = min(dt0, nf * tmp[l])
+            if t + dt0 > stop - 1e-3 * dt0:
+                dt0 = stop - t
+            dts = [dt0]
+            for l in range(1, nlev):
+                dts.append(dts[-1] / ratio[l])
+            abi.check("amr", lib.mfg_boxlist_step_amr(ha, t, dt0, 1, st))
+            t += dt0
+            n += 1
+            dtp = dts
+            if t >= stop - 1e-6 * dt0:
+                break
+    s.synchronize()
+    tt, nn = C.c_double(0.0), C.c_int(0)
+    dd = (C.c_double * nlev)(*([1e100] * nlev))
+    with torch.cuda.stream(s):
+        abi.check("evolve_amr", lib.mfg_boxlist_evolve_amr(hb, 1e300, stop, 6, C.byref(tt), dd, C.byref(nn), st))
+    s.synchronize()
+    lib.mfg_boxlist_destroy(ha)
+    lib.mfg_boxlist_destroy(hb)
+    assert nn.value == n and tt.value == t and list(dd) == dtp, (nn.value, n, tt.value, t, list(dd), dtp)
+    assert n >= 3
+    for g in range(len(amr.boxes)):
+        assert np.array_equal(ma.box_state(g), mb.box_state(g)), g
