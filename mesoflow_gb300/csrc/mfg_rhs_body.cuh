@@ -570,8 +570,11 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
 // ---------------------------------------------------------------------------
 constexpr int SWEEP_SEG = 32;  // longest face segment per thread (batched launches)
 
+// Per stencil centre: the three smoothness indicators already in the form the
+// weights use, (eps + beta)^2 (each is needed by one left and one right edge),
+// and the candidate polynomials.
 struct WenoCell {
-    double bA, bB, bC, p1, p2, p3, p4;
+    double dA, dB, dC, p1, p2, p3, p4;
 };
 
 // The sweep and the per-face form must round identically, so every operation
@@ -584,9 +587,12 @@ __device__ __forceinline__ WenoCell weno_cell(double x, double y, double z) {
     const double tA = __dadd_rn(__fma_rn(-4.0, y, __dmul_rn(3.0, x)), z);
     const double tB = __fma_rn(3.0, z, __fma_rn(-4.0, y, x));
     const double q = __dsub_rn(x, z);
-    r.bA = __fma_rn(__dmul_rn(0.25, tA), tA, kt);
-    r.bB = __fma_rn(__dmul_rn(0.25, tB), tB, kt);
-    r.bC = __fma_rn(__dmul_rn(0.25, q), q, kt);
+    const double sA = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, tA), tA, kt));
+    const double sB = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, tB), tB, kt));
+    const double sC = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, q), q, kt));
+    r.dA = __dmul_rn(sA, sA);
+    r.dB = __dmul_rn(sB, sB);
+    r.dC = __dmul_rn(sC, sC);
     r.p1 = __fma_rn(11.0, z, __fma_rn(-7.0, y, __dmul_rn(2.0, x)));
     r.p2 = __fma_rn(2.0, z, __fma_rn(5.0, y, -x));
     r.p3 = __dsub_rn(__fma_rn(5.0, y, __dmul_rn(2.0, x)), z);
@@ -594,13 +600,11 @@ __device__ __forceinline__ WenoCell weno_cell(double x, double y, double z) {
     return r;
 }
 
-// Nonlinear combination of one edge: indicators b2, b1, b0 with linear
-// weights 1, 6, 3 and candidates v2, v1, v0 (divided by 6).  The weight sum
-// is a positive normal number, so a Newton-refined reciprocal replaces the
-// division.
-__device__ __forceinline__ double weno_comb(double b2, double b1, double b0, double v2, double v1, double v0) {
-    const double s2 = __dadd_rn(kEpsWeno, b2), s1 = __dadd_rn(kEpsWeno, b1), s0 = __dadd_rn(kEpsWeno, b0);
-    const double d2 = __dmul_rn(s2, s2), d1 = __dmul_rn(s1, s1), d0 = __dmul_rn(s0, s0);
+// Nonlinear combination of one edge: (eps + beta)^2 of the three candidates
+// d2, d1, d0 with linear weights 1, 6, 3 and candidates v2, v1, v0 (divided
+// by 6).  The weight sum is a positive normal number, so a Newton-refined
+// reciprocal replaces the division.
+__device__ __forceinline__ double weno_comb(double d2, double d1, double d0, double v2, double v1, double v0) {
     const double e2 = __dmul_rn(d1, d0), e1 = __dmul_rn(6.0, __dmul_rn(d2, d0)), e0 = __dmul_rn(3.0, __dmul_rn(d2, d1));
     const double num = __fma_rn(e0, v0, __fma_rn(e1, v1, __dmul_rn(e2, v2)));
     const double den = __dadd_rn(__dadd_rn(e2, e1), e0);
@@ -673,10 +677,10 @@ __device__ __forceinline__ double flux5_face(const RhsBox& B, int d, int c, cons
         const double lam = FS.p[qf + FS_LAMBDA * FS.ns];
         double fp, fm, up, um;
         if (!(flags & 2)) {
-            fp = weno_comb(w.f0.bB, w.f1.bC, w.f2.bA, w.f0.p1, w.f1.p2, w.f2.p3);
-            fm = weno_comb(w.f3.bA, w.f2.bC, w.f1.bB, w.f3.p4, w.f2.p3, w.f1.p2);
-            up = weno_comb(w.u0.bB, w.u1.bC, w.u2.bA, w.u0.p1, w.u1.p2, w.u2.p3);
-            um = weno_comb(w.u3.bA, w.u2.bC, w.u1.bB, w.u3.p4, w.u2.p3, w.u1.p2);
+            fp = weno_comb(w.f0.dB, w.f1.dC, w.f2.dA, w.f0.p1, w.f1.p2, w.f2.p3);
+            fm = weno_comb(w.f3.dA, w.f2.dC, w.f1.dB, w.f3.p4, w.f2.p3, w.f1.p2);
+            up = weno_comb(w.u0.dB, w.u1.dC, w.u2.dA, w.u0.p1, w.u1.p2, w.u2.p3);
+            um = weno_comb(w.u3.dA, w.u2.dC, w.u1.dB, w.u3.p4, w.u2.p3, w.u1.p2);
         } else {
             weno_collapsed(fL, fR, fp, fm);
             weno_collapsed(uL, uR, up, um);
