@@ -26,6 +26,7 @@
 // foextrap, wall, or ext_dir with a velocity inlet or a fixed state.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -350,6 +351,180 @@ __global__ void __launch_bounds__(AT, 4) adj_flux_kernel(AdjBox A, int d) {
         if (c >= 1 && c <= 3) aadd(&GA.p[ox + (AUX_VX + c - 1) * GA.ns], vab);
         aadd(&GA.p[ox + AUX_PF * GA.ns], pb);
     }
+}
+
+// Adjoint of one stencil cell's Euler flux of component c and of its state
+// value (consprim_funcs.H:48-81 reversed), given the summed adjoints fb of the
+// flux and ub of the state value from the WENO5 edges.
+__device__ __forceinline__ void euler_vjp_scatter(const AdjBox& A, int c, int d, int sc, int64_t os, int64_t ox,
+                                                  double u, double fb, double ub) {
+    const RhsBox& B = A.B;
+    const Fab& S = B.sb;
+    const Fab& X = B.aux;
+    const Fab& G = A.lamSb;
+    const Fab& GA = A.lamAux;
+    const double vd = X.p[ox + (AUX_VX + d) * X.ns];
+    double rb = 0.0, vab = 0.0, vdb = 0.0, pb = 0.0, Eb = 0.0;
+    if (c == RHO) {
+        rb = fb * vd;
+        vdb = fb * u;
+    } else if (c <= RHOW) {
+        const double rho = S.p[os + RHO * S.ns], va = X.p[ox + (AUX_VX + c - 1) * X.ns];
+        rb = fb * va * vd;
+        vab = fb * rho * vd;
+        vdb = fb * rho * va;
+        if (c - 1 == d) pb = fb;
+    } else if (c == RHOE) {
+        Eb = fb * vd;
+        pb = fb * vd;
+        vdb = fb * (u + X.p[ox + AUX_PF * X.ns]);
+    } else {
+        ub += fb * vd;
+        vdb = fb * u;
+    }
+    if (c == RHO) ub += rb;
+    if (c == RHOE) ub += Eb;
+    aadd(&G.p[os + sc * G.ns], ub);
+    if (c != RHO) aadd(&G.p[os + RHO * G.ns], rb);
+    if (c != RHOE) aadd(&G.p[os + RHOE * G.ns], Eb);
+    aadd(&GA.p[ox + (AUX_VX + d) * GA.ns], vdb);
+    if (c >= 1 && c <= 3) aadd(&GA.p[ox + (AUX_VX + c - 1) * GA.ns], vab);
+    aadd(&GA.p[ox + AUX_PF * GA.ns], pb);
+}
+
+// Column-sweep form of adj_flux_kernel: one thread per (segment of seg faces
+// along d in one column, advected component c).  A window of the six stencil
+// cells slides with the face; each cell's state value and Euler flux are
+// evaluated once, the edge adjoints of the faces that use the cell are summed
+// in registers, and the Euler-flux reversal and its atomic scatter run once
+// per cell as it leaves the window (cells at the segment ends also receive
+// the neighbouring segments' sums, so the scatter stays atomic).  Same
+// mathematics as the per-face form; the order of the summation differs.
+template <int NS>
+__device__ __forceinline__ void adj_flux_sweep_body(const AdjBox& A, int d, int seg, int c, int64_t t) {
+    const RhsBox& B = A.B;
+    int ta, tb;
+    sweep_dirs(d, ta, tb);
+    const int na = B.hi[ta] - B.lo[ta] + 1, nb = B.hi[tb] - B.lo[tb] + 1;
+    const int nseg = sweep_nseg(B, d, seg);
+    if (t >= (int64_t)na * nb * nseg) return;
+    int ia, ib, is;
+    split3(t, na, nb, ia, ib, is);
+    const int nfd = B.hi[d] - B.lo[d] + 2;
+    const int f0 = B.lo[d] + is * seg, f1 = B.lo[d] + min(nfd, (is + 1) * seg);  // faces [f0, f1)
+    const DevParams& P = c_P;
+    const int sc = (c < NCONS) ? c : c + (NFLO - NCONS);
+    const Fab& S = B.sb;
+    const Fab& X = B.aux;
+    const Fab& G = A.lamSb;
+    const Fab& FS = B.fs[d];
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int64_t xd = (d == 0) ? 1 : (d == 1) ? X.js : X.ks;
+    Idx3 f;
+    int* fc[3] = {&f.i, &f.j, &f.k};
+    *fc[ta] = B.lo[ta] + ia;
+    *fc[tb] = B.lo[tb] + ib;
+    *fc[d] = f0;
+    // window: position q holds cell (face - 3 + q)
+    double us[6], fl[6], usb[6], flb[6];
+    const int64_t oR0 = S.off(f.i, f.j, f.k), xR0 = X.off(f.i, f.j, f.k);
+    auto load = [&](int q, int64_t os, int64_t ox) {
+        us[q] = S.p[os + sc * S.ns];
+        const double va = (c >= 1 && c <= 3) ? X.p[ox + (AUX_VX + c - 1) * X.ns] : 0.0;
+        fl[q] = euler_flux(c, d, us[q], S.p[os + RHO * S.ns], va, X.p[ox + (AUX_VX + d) * X.ns],
+                           X.p[ox + AUX_PF * X.ns], S.p[os + RHOE * S.ns]);
+        usb[q] = 0.0;
+        flb[q] = 0.0;
+    };
+#pragma unroll
+    for (int q = 0; q < 6; ++q) load(q, oR0 + (q - 3) * sd, xR0 + (q - 3) * xd);
+    for (int fd = f0; fd < f1; ++fd) {
+        *fc[d] = fd;
+        const int64_t oR = oR0 + (fd - f0) * sd, oL = oR - sd, xR = xR0 + (fd - f0) * xd;
+        const double Fb = face_bar(B, A.lamL, f, d, sc);
+        if (Fb != 0.0) {
+            if (c == RHOE) {  // heat conduction F_E -= k (T_R - T_L)/dx, on every face
+                const double kb = P.cond_hm * B.idx[d] * Fb;
+                aadd(&G.p[oR + TEMP * G.ns], -kb);
+                aadd(&G.p[oL + TEMP * G.ns], kb);
+            }
+            if (c >= NCONS) {  // species diffusion F_s -= D (c_R - c_L)/dx, on every face
+                const int s = c - NCONS;
+                const double* vf = S.p + VFRAC * S.ns;
+                const double Dh = (P.diff_mode[s] == MFG_TRANSPORT_CONST)
+                                      ? P.diff_hm[s]
+                                      : harmonic_mean(blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oL]),
+                                                      blend(P.diff_mode[s], P.diff_gas[s], P.diff_solid[s], vf[oR]));
+                const double v = Dh * B.idx[d] * Fb;
+                aadd(&G.p[oR + sc * G.ns], -v);
+                aadd(&G.p[oL + sc * G.ns], v);
+            }
+            const int64_t qf = FS.off(f.i, f.j, f.k);
+            const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
+            const double hb = (c < NCONS) ? Fb : P.advect_flag[c - NCONS] * Fb;
+            if ((flags & 1) && hb != 0.0) {
+                const bool fallback = flags & 2;
+                const double lam = FS.p[qf + FS_LAMBDA * FS.ns];
+                // the same four edge reversals for every lane (with the first-order
+                // fallback the six stencil entries are the two face cells), then the
+                // stencil adjoints are added to the window, collapsed for the fallback
+                double sf[6], su[6];
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const int w = fallback ? ((q < 3) ? 2 : 3) : q;
+                    sf[q] = fl[w];
+                    su[q] = us[w];
+                }
+                double gf[6] = {0, 0, 0, 0, 0, 0}, gu[6] = {0, 0, 0, 0, 0, 0};
+                EdgeGrad g;
+                weno_edge_vjp(sf[0], sf[1], sf[2], sf[3], sf[4], 0.5 * hb, g);
+                gf[0] += g.a; gf[1] += g.b; gf[2] += g.c; gf[3] += g.d; gf[4] += g.e;
+                weno_edge_vjp(sf[5], sf[4], sf[3], sf[2], sf[1], 0.5 * hb, g);
+                gf[5] += g.a; gf[4] += g.b; gf[3] += g.c; gf[2] += g.d; gf[1] += g.e;
+                const double up = weno_edge_vjp(su[0], su[1], su[2], su[3], su[4], 0.5 * lam * hb, g);
+                gu[0] += g.a; gu[1] += g.b; gu[2] += g.c; gu[3] += g.d; gu[4] += g.e;
+                const double um = weno_edge_vjp(su[5], su[4], su[3], su[2], su[1], -0.5 * lam * hb, g);
+                gu[5] += g.a; gu[4] += g.b; gu[3] += g.c; gu[2] += g.d; gu[1] += g.e;
+                if (fallback) {
+                    flb[2] += (gf[0] + gf[1]) + gf[2];
+                    flb[3] += (gf[3] + gf[4]) + gf[5];
+                    usb[2] += (gu[0] + gu[1]) + gu[2];
+                    usb[3] += (gu[3] + gu[4]) + gu[5];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        flb[q] += gf[q];
+                        usb[q] += gu[q];
+                    }
+                }
+                aadd(&FS.p[qf + FS_MH * FS.ns], 0.5 * hb * (up - um));
+            }
+        }
+        if (fd + 1 < f1) {  // cell fd - 3 leaves the window; cell fd + 3 enters
+            if (usb[0] != 0.0 || flb[0] != 0.0)
+                euler_vjp_scatter(A, c, d, sc, oR - 3 * sd, xR - 3 * xd, us[0], flb[0], usb[0]);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                us[q] = us[q + 1];
+                fl[q] = fl[q + 1];
+                usb[q] = usb[q + 1];
+                flb[q] = flb[q + 1];
+            }
+            load(5, oR + 3 * sd, xR + 3 * xd);
+        }
+    }
+    const int64_t oR = oR0 + (f1 - 1 - f0) * sd, xR = xR0 + (f1 - 1 - f0) * xd;
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        if (usb[q] != 0.0 || flb[q] != 0.0)
+            euler_vjp_scatter(A, c, d, sc, oR + (q - 3) * sd, xR + (q - 3) * xd, us[q], flb[q], usb[q]);
+}
+
+// Every box of a stage in one launch (blockIdx.z = box): the boxes' adjoint
+// accumulations are disjoint, and one box alone leaves too few columns.
+template <int NS>
+__global__ void __launch_bounds__(AT, 3) adj_flux_sweep_kernel(const AdjBox* __restrict__ boxes, int d, int seg) {
+    adj_flux_sweep_body<NS>(boxes[blockIdx.z], d, seg, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // One thread per face of direction d: viscous stress (F_{m_a} -= tau_a,
@@ -1118,6 +1293,7 @@ struct Work {
     int* d_owner = nullptr;
     int gran = 1, mlen[3] = {1, 1, 1};
     CopyTab* d_tab = nullptr;  // [nbox] -> lam, [nbox] -> lamOld
+    AdjBox* d_adj = nullptr;   // the stage's AdjBox views of every box (batched adjoint flux)
     double* d_scratch = nullptr;
     int* d_list = nullptr;
     unsigned* d_count = nullptr;
@@ -1134,6 +1310,7 @@ struct Work {
         cudaFree(d_list);
         cudaFree(d_count);
         cudaFree(d_g);
+        cudaFree(d_adj);
         cudaFree(d_cutlist);
         cudaFree(d_cutcount);
     }
@@ -1205,6 +1382,16 @@ cudaError_t copy_region(const Fab& dst, const Fab& src, const int lo[3], const i
     copy_box_kernel<<<g, 256, 0, st>>>(dst, src, v, nc);
     return cudaGetLastError();
 }
+
+// Form of the adjoint flux kernel: column sweep (default) or the per-face
+// form of the same mathematics (MFG_ADJ_FLUX_PER_FACE=1 in the environment;
+// the tests compare the two).
+bool adj_flux_sweep() {
+    const char* e = getenv("MFG_ADJ_FLUX_PER_FACE");
+    return !(e && e[0] == '1');
+}
+
+constexpr int kAdjSeg = 16;  // faces per column segment of the batched adjoint flux sweep
 
 // Forward intermediates of one step.
 struct Snap {
@@ -1307,22 +1494,39 @@ int adj_step(Work& W, double dt, const Snap& sn, double* lam, double* lamOld, do
                                                 W.gfab(lamSb, b, N), W.gfab(sb, b, N), stage, dt, N);
             ADJ_TRY(cudaGetLastError(), "reverse: stage algebra");
         }
+        // forward views of the stage for every box: its state, per-cell primitives
+        // and face scalars as the forward computed them
+        std::vector<AdjBox> adj(W.nbox);
         for (int b = 0; b < W.nbox; ++b) {
             mfg_box x = W.boxes[b];
             x.sborder = W.ga4(sb, b);
-            AdjBox A;
-            // forward views of the stage: its state, per-cell primitives and face
-            // scalars as the forward computed them
+            AdjBox& A = adj[b];
             A.B = layout_rhs_box(x, W.g, W.d_scratch);
             snap_views(W, A.B, sn, stage, b);
             A.lamL = W.vfab(lamL, b);
             A.lamSb = W.gfab(lamSb, b, N);
             A.lamAux = W.gfab(lamAux, b, NAUX);
+        }
+        const int C = NCONS + c_host_params().nspec;
+        const bool sweep = adj_flux_sweep();
+        if (sweep) {  // hyperbolic fluxes of all boxes, one column-sweep launch per direction
+            ADJ_TRY(cudaMemcpyAsync(W.d_adj, adj.data(), W.nbox * sizeof(AdjBox), cudaMemcpyHostToDevice, st),
+                    "reverse: box views");
+            for (int d = 0; d < 3; ++d) {
+                unsigned nbs = 1;
+                for (int b = 0; b < W.nbox; ++b) nbs = std::max(nbs, nblk(sweep_items(adj[b].B, d, kAdjSeg), AT));
+                ProfScope ps(K_ADJ_FLUX, st);
+                ADJ_NS(adj_flux_sweep_kernel, (dim3(nbs, C, W.nbox), AT, 0, st), (W.d_adj, d, kAdjSeg));
+                ADJ_TRY(cudaGetLastError(), "reverse: face fluxes");
+            }
+        }
+        for (int b = 0; b < W.nbox; ++b) {
+            const AdjBox& A = adj[b];
+            const mfg_box& x = W.boxes[b];
             const int64_t ng = W.grown_cells(b);
-            const int C = NCONS + c_host_params().nspec;
             for (int d = 0; d < 3; ++d) {
                 const unsigned nbf = nblk(face_items(A.B, d), AT);
-                {
+                if (!sweep) {
                     ProfScope ps(K_ADJ_FLUX, st);
                     ADJ_NS(adj_flux_kernel, (dim3(nbf, C), AT, 0, st), (A, d));
                 }
@@ -1464,6 +1668,7 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
     ADJ_TRY(cudaMalloc(&W.d_count, 256), "allocation");
     ADJ_TRY(cudaMalloc(&W.d_g, (2 + MAXR) * sizeof(double)), "allocation");
     ADJ_TRY(cudaMalloc(&W.d_tab, 2 * (size_t)nbox * sizeof(CopyTab)), "allocation");
+    ADJ_TRY(cudaMalloc(&W.d_adj, (size_t)std::max(nbox, 1) * sizeof(AdjBox)), "allocation");
     ADJ_TRY(cudaMemsetAsync(W.d_g, 0, (2 + MAXR) * sizeof(double), st), "clear");
     // cut-cell lists of every box (from the volume fraction of s_new)
     ADJ_TRY(cudaMalloc(&W.d_cutlist, std::max<size_t>(W.vtot, 1) * sizeof(int)), "allocation");
