@@ -111,6 +111,9 @@ extern "C" {
 #define MFG_EXT_PRESSURE_OUTLET  2  /* pres fixed; dens,velocity,species from the interior
                                        (models/porousParticle/externbc.H:44-58) */
 #define MFG_EXT_VELOCITY_INLET   3  /* dens,velocity,pres,species fixed (conserved from prim) */
+#define MFG_EXT_SPECIES_DIRICHLET 4 /* flow components from the interior, vfrac 1, species
+                                       2 spec - s_int (boundary value spec on the face)
+                                       (tests/Cartesian/SpeciesEqTests/externbc.H:20-52) */
 
 /* ---- views ---------------------------------------------------------------- */
 /* Mirror of amrex::Array4<Real>: p[(i-begin0) + (j-begin1)*jstride

@@ -23,7 +23,7 @@ THERMO_MOLAR, THERMO_MASS_SINGLE, THERMO_BG_GAS = 0, 1, 2
 EFORM_MOLAR_CV, EFORM_MASS_CV = 0, 1
 TRANSPORT_CONST, TRANSPORT_VFRAC_BLEND = 0, 1
 BC_INT_DIR, BC_FOEXTRAP, BC_EXT_DIR, BC_WALL = 0, 2, 3, 6
-EXT_FIXED_STATE, EXT_PRESSURE_INLET, EXT_PRESSURE_OUTLET, EXT_VELOCITY_INLET = 0, 1, 2, 3
+EXT_FIXED_STATE, EXT_PRESSURE_INLET, EXT_PRESSURE_OUTLET, EXT_VELOCITY_INLET, EXT_SPECIES_DIRICHLET = 0, 1, 2, 3, 4
 
 ERROR_NAMES = {
     OK: "ok", ERR_ARG: "bad argument", ERR_NAN: "NaN detected in dsdt",

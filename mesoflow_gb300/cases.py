@@ -157,6 +157,53 @@ def sod(n_cell=(256, 4, 4), order=5, max_grid=64, axis=0):
     return Case("sod", P, n_cell, (0, 0, 0), prob_hi, periodic, max_grid, S, {"axis": axis})
 
 
+def species_eq(n=32, max_grid=16, axis=0):
+    """tests/Cartesian/SpeciesEqTests: the flow is frozen (solve_navier_stokes
+    = 0) at rho = p = 1 (mass-single thermo, R = 1, gamma 1.4) with unit
+    velocity along `axis`; S1 is advected and diffused (D = 0.1) between the
+    boundary values 0 and 1, S2 is only diffused (D = 1, advect flag 0) with a
+    unit source and zero boundary values (ext_dir faces whose ghost species
+    are reflected about the value, externbc.H; walls across).  Steady state:
+    S1 = (exp(x/0.1) - 1)/(exp(10) - 1), S2 = x(1 - x)/2."""
+    P = _base_params(2)
+    P.thermo_kind = abi.THERMO_MASS_SINGLE
+    P.gas_R = 1.0
+    P.gamma_single = 1.4
+    P.ngas = 2
+    P.molwt[0], P.molwt[1] = 0.032, 0.028
+    P.advect_flag[0], P.advect_flag[1] = 1.0, 0.0
+    for s, D in enumerate((0.1, 1.0)):
+        P.diff_mode[s] = abi.TRANSPORT_CONST
+        P.diff_gas[s] = D
+    P.visc_gas = 0.01
+    P.cond_gas = 0.0
+    P.do_ns = 0
+    P.cfl = 0.8
+    P.chem_on = 1
+    P.nreact = 1
+    P.nu[0][1] = 1.0       # S2 source 1: a reaction with no reactants and rate constant 1
+    P.A[0] = 1.0
+    for d in range(3):
+        if d == axis:
+            P.bc_lo[d] = P.bc_hi[d] = abi.BC_EXT_DIR
+        else:
+            P.bc_lo[d] = P.bc_hi[d] = abi.BC_WALL
+    for e, (s1, s2) in ((P.ext_lo[axis], (0.0, 0.0)), (P.ext_hi[axis], (1.0, 0.0))):
+        e.kind = abi.EXT_SPECIES_DIRICHLET
+        e.spec[0], e.spec[1] = s1, s2
+    n_cell = [4, 4, 4]
+    n_cell[axis] = n
+    prob_hi = [0.125, 0.125, 0.125]
+    prob_hi[axis] = 1.0
+    shape = (n_cell[2], n_cell[1], n_cell[0])
+    one = np.ones(shape)
+    zero = np.zeros(shape)
+    vel = [zero, zero, zero]
+    vel[axis] = one
+    S = state_from_prim(P, one, vel[0], vel[1], vel[2], one, [zero, zero], one)
+    return Case("species_eq", P, n_cell, (0, 0, 0), prob_hi, (0, 0, 0), max_grid, S, {"axis": axis})
+
+
 def taylor_green_mix(n=256, order=5, max_grid=64, seed=20261203, v0=10.0):
     """3D Taylor-Green vortex on [-1,1]^3 (velocity of tests/Cartesian/TaylorGreen/
     Prob.H) plus 1% Gaussian noise, in a 5-species calorically perfect molar

@@ -22,6 +22,12 @@ __device__ void external_state(const mfg_extbc& E, int idir, const double* s_int
         if (E.keep_interior_pres) s_ext[PRES] = s_int[PRES];
         return;
     }
+    if (E.kind == MFG_EXT_SPECIES_DIRICHLET) {
+        for (int n = 0; n < NFLO && n < nc; ++n) s_ext[n] = s_int[n];
+        s_ext[VFRAC] = 1.0;
+        for (int s = 0; s < ns; ++s) s_ext[NFLO + s] = __dsub_rn(__dmul_rn(2.0, E.spec[s]), s_int[NFLO + s]);
+        return;
+    }
     double spec[NS];
     double dens, pres, vel[3];
     if (E.kind == MFG_EXT_PRESSURE_INLET) {

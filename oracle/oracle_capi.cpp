@@ -101,6 +101,14 @@ void externalbc(const Ctx& c, const mfg_extbc& E, const double* s_int, double* s
         if (E.keep_interior_pres) s_ext[PRES_INDX] = s_int[PRES_INDX];
         return;
     }
+    if (E.kind == MFG_EXT_SPECIES_DIRICHLET) {
+        // tests/Cartesian/SpeciesEqTests/externbc.H:20-52: flow from the
+        // interior, vfrac one, species reflected about the boundary value
+        for (int n = 0; n < FLO_NVARS; n++) s_ext[n] = s_int[n];
+        s_ext[VFRAC_INDX] = one;
+        for (int sp = 0; sp < ns; sp++) s_ext[FLO_NVARS + sp] = two * E.spec[sp] - s_int[FLO_NVARS + sp];
+        return;
+    }
     double spec_ext[MAXS];
     double dens, pres, vel[3];
     if (E.kind == MFG_EXT_PRESSURE_INLET) {

@@ -174,3 +174,34 @@ def test_oracle_ros2_stiff_decay():
     a0 = o.level.s_new[0][abi.FLO_NVARS].copy()
     assert o.lib.oracle_chem_substep_ros2(C.byref(c.params), o.desc, 1, 1e-6, 1e-6, 1e-12, 2000) == 0
     assert np.allclose(o.level.s_new[0][abi.FLO_NVARS], a0 * np.exp(-0.5), rtol=2e-5, atol=0)
+
+
+def _species_eq_exact(n):
+    x = (np.arange(n) + 0.5) / n
+    return x, (np.exp(x / 0.1) - 1) / (np.exp(10.0) - 1), 0.5 * (x - x * x)
+
+
+def test_oracle_species_equations_reach_the_analytic_steady_state():
+    """tests/Cartesian/SpeciesEqTests (its inputs_x, externbc.H, chemistry.H,
+    verify_spec.py): frozen flow, S1 advected (u = 1) and diffused (D = 0.1)
+    between 0 and 1, S2 diffused (D = 1) with a unit source, run to t = 1 with
+    CFL 0.8 on 32 cells.  S2 matches x(1-x)/2 to 0.2% of its maximum.  S1 is
+    advected first-order upwind (the scalar MUSCL call takes its states by
+    value, compute_flux_3d.H:403), so it matches the exact solution of that
+    scheme's modified equation (D + u dx/2) to 1e-2 and the continuous one to
+    5e-2."""
+    c = cases.species_eq(n=32)
+    o = OracleLevel(c)
+    while o.time < 1.0 - 1e-12:
+        o.advance(o.compute_dt(stop_time=1.0))
+    s = o.state()
+    x, e1, e2 = _species_eq_exact(32)
+    s1 = s[abi.FLO_NVARS][2, 2, :]
+    s2 = s[abi.FLO_NVARS + 1][2, 2, :]
+    assert np.abs(s2 - e2).max() < 2e-3 * e2.max()
+    deff = 0.1 + 0.5 / 32
+    e1m = (np.exp(x / deff) - 1) / (np.exp(1 / deff) - 1)
+    assert np.abs(s1 - e1m).max() < 1e-2
+    assert np.abs(s1 - e1).max() < 5e-2
+    # the frozen flow stays as initialised
+    assert np.array_equal(s[abi.RHO], c.state[abi.RHO]) and np.array_equal(s[abi.RHOU], c.state[abi.RHOU])

@@ -38,12 +38,17 @@ def small(name):
         return perturb(cases.catalyst(n=16, order=5, max_grid=8), 8, vel_amp=1e-2)
     if name == "cat2":
         return perturb(cases.catalyst(n=16, order=2, max_grid=8), 9, vel_amp=1e-2)
+    if name == "speq":  # frozen flow (no Navier-Stokes terms), species Dirichlet ends, a constant source
+        c = cases.species_eq(n=32, max_grid=8)
+        rng = np.random.default_rng(11)
+        c.state[abi.FLO_NVARS:abi.FLO_NVARS + 2] = rng.uniform(0.0, 1.0, size=(2,) + c.state.shape[1:])
+        return c
     if name == "catbg5":
         return perturb(cases.catalyst(n=16, order=5, max_grid=8, bg_gas=True), 10, vel_amp=1e-2)
     raise KeyError(name)
 
 
-NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2", "catbg5"]
+NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2", "catbg5", "speq"]
 
 
 class Gpu:
@@ -142,7 +147,7 @@ def test_one_step_parity(name):
     assert np.all(np.abs(rg - ro) <= 1e-9 * np.abs(ro) + TOL_STEP * scale)
 
 
-@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5", "catbg5"])
+@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5", "catbg5", "speq"])
 def test_multistep_l2(name):
     c = small(name)
     o, g = oracle_for(c), Gpu(c)
@@ -203,3 +208,21 @@ def test_bad_box_rejected():
     d[0] = g.desc[0]
     d[0].sborder.begin[0] += 1  # ghost region no longer covered
     assert g.lib.mfg_compute_dsdt_flow(d, 1, g.g, 0.0, 1e-6, g.st) == abi.ERR_ARG
+
+
+def test_species_equations_reach_the_analytic_steady_state():
+    """The GPU on tests/Cartesian/SpeciesEqTests run to t = 1 (its own dt
+    sequence): the same bounds as the oracle's run against x(1-x)/2 and the
+    upwind scheme's steady state (tests/test_cpu_oracle.py)."""
+    from mesoflow_gb300.driver import Mflo
+    c = cases.species_eq(n=32)
+    g = Mflo(c, device="cuda")
+    while g.time < 1.0 - 1e-12:
+        g.advance(g.compute_dt(stop_time=1.0), norms=False)
+    s = g.state()
+    x = (np.arange(32) + 0.5) / 32
+    e2 = 0.5 * (x - x * x)
+    deff = 0.1 + 0.5 / 32
+    e1m = (np.exp(x / deff) - 1) / (np.exp(1 / deff) - 1)
+    assert np.abs(s[abi.FLO_NVARS + 1][2, 2, :] - e2).max() < 2e-3 * e2.max()
+    assert np.abs(s[abi.FLO_NVARS][2, 2, :] - e1m).max() < 1e-2
