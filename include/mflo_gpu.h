@@ -111,9 +111,11 @@ extern "C" {
 #define MFG_EXT_PRESSURE_OUTLET  2  /* pres fixed; dens,velocity,species from the interior
                                        (models/porousParticle/externbc.H:44-58) */
 #define MFG_EXT_VELOCITY_INLET   3  /* dens,velocity,pres,species fixed (conserved from prim) */
-#define MFG_EXT_SPECIES_DIRICHLET 4 /* flow components from the interior, vfrac 1, species
-                                       2 spec - s_int (boundary value spec on the face)
-                                       (tests/Cartesian/SpeciesEqTests/externbc.H:20-52) */
+#define MFG_EXT_SPECIES_DIRICHLET 4 /* flow components from the interior, vfrac 1 (or from the
+                                       interior), species 2 spec - s_int (value spec on the face)
+                                       or zero gradient per species
+                                       (tests/Cartesian/SpeciesEqTests/externbc.H:20-52,
+                                       models/blockCatalyst1d/externbc.H:18-55) */
 
 /* ---- views ---------------------------------------------------------------- */
 /* Mirror of amrex::Array4<Real>: p[(i-begin0) + (j-begin1)*jstride
@@ -153,6 +155,8 @@ typedef struct mfg_geom {
 typedef struct mfg_extbc {
     int    kind;                  /* MFG_EXT_* */
     int    keep_interior_pres;    /* FIXED_STATE: PRES_INDX copied from the boundary cell */
+    int    spec_zero_grad_mask;   /* SPECIES_DIRICHLET: bit s set = species s copied from the boundary cell */
+    int    vfrac_interior;        /* SPECIES_DIRICHLET: VFRAC copied from the boundary cell (else 1) */
     double dens, pres;
     double vel[3];
     double spec[MFG_MAX_SPECIES];

@@ -49,7 +49,8 @@ class Geom(C.Structure):
 
 
 class ExtBC(C.Structure):
-    _fields_ = [("kind", C.c_int), ("keep_interior_pres", C.c_int), ("dens", C.c_double), ("pres", C.c_double),
+    _fields_ = [("kind", C.c_int), ("keep_interior_pres", C.c_int), ("spec_zero_grad_mask", C.c_int),
+                ("vfrac_interior", C.c_int), ("dens", C.c_double), ("pres", C.c_double),
                 ("vel", C.c_double * 3), ("spec", C.c_double * MAX_SPECIES),
                 ("state", C.c_double * (FLO_NVARS + MAX_SPECIES))]
 

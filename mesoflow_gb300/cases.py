@@ -204,6 +204,56 @@ def species_eq(n=32, max_grid=16, axis=0):
     return Case("species_eq", P, n_cell, (0, 0, 0), prob_hi, (0, 0, 0), max_grid, S, {"axis": axis})
 
 
+def block_catalyst_1d(n=32, max_grid=16, l1=0.7):
+    """models/blockCatalyst1d: frozen flow at rho = p = 1 (mass-single, R = 1,
+    gamma 1.4); gas for x < l1 with unit velocity, a catalyst block beyond
+    (vfrac by 8-corner sampling, velocity 0 where vfrac < 1, site
+    concentration 1 - vfrac); S1 (D = 0.5) is 1 at x = 0 and 0 at x = 1, S2
+    (D = 1) has zero gradient at both ends, site species not transported; the
+    surface reaction S1 + site -> S2 + site with rate 5 [site][S1].  Steady S1:
+    the piecewise analytic solution of verify_spec.py."""
+    P = _base_params(3)
+    P.thermo_kind = abi.THERMO_MASS_SINGLE
+    P.gas_R = 1.0
+    P.gamma_single = 1.4
+    P.ngas = 2
+    for s, (W, adv, D) in enumerate(((0.032, 1.0, 0.5), (0.028, 1.0, 1.0), (0.001, 0.0, 0.0))):
+        P.molwt[s], P.advect_flag[s] = W, adv
+        P.diff_mode[s] = abi.TRANSPORT_CONST
+        P.diff_gas[s] = D
+    P.visc_gas = 0.01
+    P.cond_gas = 0.0
+    P.do_ns = 0
+    P.species_in_solid = 1
+    P.cfl = 0.8
+    P.chem_on = 1
+    P.nreact = 1
+    P.nu[0][0], P.nu[0][1] = -1.0, 1.0
+    P.order[0][0], P.order[0][2] = 1.0, 1.0
+    P.A[0] = 5.0
+    P.bc_lo[0] = P.bc_hi[0] = abi.BC_EXT_DIR
+    for d in (1, 2):
+        P.bc_lo[d] = P.bc_hi[d] = abi.BC_WALL
+    for e, s1 in ((P.ext_lo[0], 1.0), (P.ext_hi[0], 0.0)):
+        e.kind = abi.EXT_SPECIES_DIRICHLET
+        e.spec[0] = s1
+        e.spec_zero_grad_mask = 0b010   # S2 zero gradient
+        e.vfrac_interior = 1
+    n_cell = (n, 4, 4)
+    prob_hi = (1.0, 0.125, 0.125)
+    dx = 1.0 / n
+    xc = np.arange(n + 1) * dx                                  # cell corners along x
+    frac = np.array([0.5 * (float(xc[i] < l1) + float(xc[i + 1] < l1)) for i in range(n)])
+    shape = (4, 4, n)
+    vf = np.broadcast_to(frac, shape).copy()
+    one = np.ones(shape)
+    zero = np.zeros(shape)
+    u = np.where(vf < 1.0, 0.0, 1.0)
+    spec = [zero, zero, 1.0 - vf]
+    S = state_from_prim(P, one, u, zero, zero, one, spec, vf)
+    return Case("block_catalyst_1d", P, n_cell, (0, 0, 0), prob_hi, (0, 0, 0), max_grid, S, {"l1": l1})
+
+
 def taylor_green_mix(n=256, order=5, max_grid=64, seed=20261203, v0=10.0):
     """3D Taylor-Green vortex on [-1,1]^3 (velocity of tests/Cartesian/TaylorGreen/
     Prob.H) plus 1% Gaussian noise, in a 5-species calorically perfect molar

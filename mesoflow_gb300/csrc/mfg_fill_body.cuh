@@ -24,8 +24,11 @@ __device__ void external_state(const mfg_extbc& E, int idir, const double* s_int
     }
     if (E.kind == MFG_EXT_SPECIES_DIRICHLET) {
         for (int n = 0; n < NFLO && n < nc; ++n) s_ext[n] = s_int[n];
-        s_ext[VFRAC] = 1.0;
-        for (int s = 0; s < ns; ++s) s_ext[NFLO + s] = __dsub_rn(__dmul_rn(2.0, E.spec[s]), s_int[NFLO + s]);
+        if (!E.vfrac_interior) s_ext[VFRAC] = 1.0;
+        for (int s = 0; s < ns; ++s)
+            s_ext[NFLO + s] = ((E.spec_zero_grad_mask >> s) & 1)
+                                  ? s_int[NFLO + s]
+                                  : __dsub_rn(__dmul_rn(2.0, E.spec[s]), s_int[NFLO + s]);
         return;
     }
     double spec[NS];

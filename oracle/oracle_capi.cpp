@@ -104,9 +104,12 @@ void externalbc(const Ctx& c, const mfg_extbc& E, const double* s_int, double* s
     if (E.kind == MFG_EXT_SPECIES_DIRICHLET) {
         // tests/Cartesian/SpeciesEqTests/externbc.H:20-52: flow from the
         // interior, vfrac one, species reflected about the boundary value
+        // (models/blockCatalyst1d/externbc.H:18-55 keeps VFRAC and copies S2)
         for (int n = 0; n < FLO_NVARS; n++) s_ext[n] = s_int[n];
-        s_ext[VFRAC_INDX] = one;
-        for (int sp = 0; sp < ns; sp++) s_ext[FLO_NVARS + sp] = two * E.spec[sp] - s_int[FLO_NVARS + sp];
+        if (!E.vfrac_interior) s_ext[VFRAC_INDX] = one;
+        for (int sp = 0; sp < ns; sp++)
+            s_ext[FLO_NVARS + sp] = ((E.spec_zero_grad_mask >> sp) & 1) ? s_int[FLO_NVARS + sp]
+                                                                       : two * E.spec[sp] - s_int[FLO_NVARS + sp];
         return;
     }
     double spec_ext[MAXS];

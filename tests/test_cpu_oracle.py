@@ -205,3 +205,31 @@ def test_oracle_species_equations_reach_the_analytic_steady_state():
     assert np.abs(s1 - e1).max() < 5e-2
     # the frozen flow stays as initialised
     assert np.array_equal(s[abi.RHO], c.state[abi.RHO]) and np.array_equal(s[abi.RHOU], c.state[abi.RHOU])
+
+
+def _block_catalyst_exact(x, v=1.0, D=0.5, k=5.0, l1=0.7, l=1.0):
+    """The piecewise steady solution of models/blockCatalyst1d/verify_spec.py
+    (advection-diffusion in the gas, diffusion-reaction in the catalyst, flux
+    continuity at l1), restated."""
+    w = np.sqrt(k / D)
+    F = 1 / (np.exp(v * l1 / D) - 1)
+    A = v * (1 + F) / (v * F * (np.exp(w * l1) - np.exp(w * (2 * l - l1))) -
+                       D * w * (np.exp(w * l1) + np.exp(w * (2 * l - l1))))
+    B = -A * np.exp(2 * w * l)
+    c1 = (A * np.exp(w * l1) + B * np.exp(-w * l1) - 1) * F
+    return np.where(x < l1, c1 * (np.exp(v * x / D) - 1) + 1, A * np.exp(w * x) + B * np.exp(-w * x))
+
+
+def test_oracle_block_catalyst_reaches_the_analytic_steady_state():
+    """models/blockCatalyst1d (inputs_x, Prob.H, chemistry.H, externbc.H,
+    verify_spec.py): gas with unit velocity up to x = 0.7, a catalyst block
+    beyond (cut cell at the interface), surface reaction S1 + site -> S2 +
+    site, run to t = 1.35: S1 within 0.025 of the piecewise analytic solution
+    on 32 cells (first-order upwind advection, one cut cell)."""
+    c = cases.block_catalyst_1d(n=32)
+    o = OracleLevel(c)
+    while o.time < 1.35 - 1e-12:
+        o.advance(o.compute_dt(stop_time=1.35))
+    x = (np.arange(32) + 0.5) / 32
+    s1 = o.state()[abi.FLO_NVARS][2, 2, :]
+    assert np.abs(s1 - _block_catalyst_exact(x)).max() < 0.025

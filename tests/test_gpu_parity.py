@@ -43,12 +43,17 @@ def small(name):
         rng = np.random.default_rng(11)
         c.state[abi.FLO_NVARS:abi.FLO_NVARS + 2] = rng.uniform(0.0, 1.0, size=(2,) + c.state.shape[1:])
         return c
+    if name == "bcat1d":  # immersed block, surface reaction, species boundary values, no Navier-Stokes terms
+        c = cases.block_catalyst_1d(n=32, max_grid=8)
+        rng = np.random.default_rng(12)
+        c.state[abi.FLO_NVARS:abi.FLO_NVARS + 2] = rng.uniform(0.0, 1.0, size=(2,) + c.state.shape[1:])
+        return c
     if name == "catbg5":
         return perturb(cases.catalyst(n=16, order=5, max_grid=8, bg_gas=True), 10, vel_amp=1e-2)
     raise KeyError(name)
 
 
-NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2", "catbg5", "speq"]
+NAMES = ["sod5", "sod2", "sod1", "sod4", "tg5", "porous2", "porous5", "cat5", "cat2", "catbg5", "speq", "bcat1d"]
 
 
 class Gpu:
@@ -147,7 +152,7 @@ def test_one_step_parity(name):
     assert np.all(np.abs(rg - ro) <= 1e-9 * np.abs(ro) + TOL_STEP * scale)
 
 
-@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5", "catbg5", "speq"])
+@pytest.mark.parametrize("name", ["sod5", "tg5", "porous2", "cat5", "catbg5", "speq", "bcat1d"])
 def test_multistep_l2(name):
     c = small(name)
     o, g = oracle_for(c), Gpu(c)
@@ -226,3 +231,16 @@ def test_species_equations_reach_the_analytic_steady_state():
     e1m = (np.exp(x / deff) - 1) / (np.exp(1 / deff) - 1)
     assert np.abs(s[abi.FLO_NVARS + 1][2, 2, :] - e2).max() < 2e-3 * e2.max()
     assert np.abs(s[abi.FLO_NVARS][2, 2, :] - e1m).max() < 1e-2
+
+
+def test_block_catalyst_reaches_the_analytic_steady_state():
+    """The GPU on models/blockCatalyst1d run to t = 1.35: S1 within 0.025 of
+    the piecewise analytic solution, as the oracle (tests/test_cpu_oracle.py)."""
+    from mesoflow_gb300.driver import Mflo
+    from test_cpu_oracle import _block_catalyst_exact
+    c = cases.block_catalyst_1d(n=32)
+    g = Mflo(c, device="cuda")
+    while g.time < 1.35 - 1e-12:
+        g.advance(g.compute_dt(stop_time=1.35), norms=False)
+    x = (np.arange(32) + 0.5) / 32
+    assert np.abs(g.state()[abi.FLO_NVARS][2, 2, :] - _block_catalyst_exact(x)).max() < 0.025
