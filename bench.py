@@ -108,6 +108,22 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time: every replica's timed region is bracketed by
+    barriers, and the whole job's throughput uses the maximum."""
+    if not dist:
+        return ms
+    import torch
+    x = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return float(x.item())
+
+
+def replica_value(cells, steps, world, ms):
+    """Whole-job cell-updates/s of N independent replicas (weak scaling)."""
+    return cells * steps * world / (ms / 1e3)
+
+
 def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=4):
     """The oracle (OpenMP build) on a bounded sample: the same workload
     generator at n=128 with 32^3 boxes; returns (cell-updates/s, threads, sample)."""
@@ -415,11 +431,8 @@ def main():
     launches = lib.mfg_launch_count() - l0
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
-    if dist:
-        x = torch.tensor([ms], device="cuda")
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms = float(x.item())
-    value = cells * a.steps * world / (ms / 1e3)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = replica_value(cells, a.steps, world, ms)
 
     # ---- end to end through the C ABI with host buffers ----------------------------
     host = [torch.empty_like(x, device="cpu").pin_memory() for x in lev.s_new]
@@ -440,12 +453,8 @@ def main():
             h.copy_(x, non_blocking=True)
     e3.record(stream)
     torch.cuda.synchronize()
-    ms_e2e = e2.elapsed_time(e3)
-    if dist:
-        x = torch.tensor([ms_e2e], device="cuda")
-        dist.all_reduce(x, op=dist.ReduceOp.MAX)
-        ms_e2e = float(x.item())
-    e2e = cells * a.steps * world / (ms_e2e / 1e3)
+    ms_e2e = max_over_ranks(e2.elapsed_time(e3), dist, "cuda")
+    e2e = replica_value(cells, a.steps, world, ms_e2e)
 
     # ---- per-kernel timing (CUDA events on the launching stream) -----------------
     lib.mfg_profile(1)

@@ -439,6 +439,12 @@ long long mfg_boxlist_cells(const mfg_boxlist* list);
  * with k_r = A_r, or A_r exp(-Ea_r/(RU T)) when Ea_r != 0 (the rate law of
  * the chemistry source, chemistry.H compute_spec_source). */
 
+/* Form of the adjoint's hyperbolic-flux reversal: 1 (default) a column sweep
+ * over all boxes of a stage (edge adjoints summed in registers, one scatter
+ * per cell), 0 one thread per face and component; the two differ only in the
+ * order of the floating-point sums. */
+int mfg_set_adjoint_flux_form(int form);
+
 /* J on the boxes' s_new.  Synchronizes. */
 int mfg_reaction_objective(const mfg_box* boxes, int nbox, const mfg_geom* geom, double* J,
                            void* stream);

@@ -117,6 +117,7 @@ SIGNATURES = [
                                          C.POINTER(C.c_double), C.POINTER(C.c_int), _VP]),
     ("mfg_chem_advance_rk2", C.c_int, [_BP, C.c_int, C.c_double, C.c_double, _VP]),
     ("mfg_set_chem_integrator", C.c_int, [C.c_int, C.c_double, C.c_double, C.c_int]),
+    ("mfg_set_adjoint_flux_form", C.c_int, [C.c_int]),
     ("mfg_store_inertgas_conc", C.c_int, [_BP, C.c_int, _VP]),
     ("mfg_update_vars_after_chemsolve", C.c_int, [_BP, C.c_int, C.c_int, _VP]),
     ("mfg_boxlist_autotune", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double), _VP]),

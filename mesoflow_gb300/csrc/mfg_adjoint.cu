@@ -1383,13 +1383,10 @@ cudaError_t copy_region(const Fab& dst, const Fab& src, const int lo[3], const i
     return cudaGetLastError();
 }
 
-// Form of the adjoint flux kernel: column sweep (default) or the per-face
-// form of the same mathematics (MFG_ADJ_FLUX_PER_FACE=1 in the environment;
-// the tests compare the two).
-bool adj_flux_sweep() {
-    const char* e = getenv("MFG_ADJ_FLUX_PER_FACE");
-    return !(e && e[0] == '1');
-}
+// Form of the adjoint flux kernel (mfg_set_adjoint_flux_form): column sweep
+// (default) or the per-face form of the same mathematics.
+int g_adj_flux_form = 1;
+bool adj_flux_sweep() { return g_adj_flux_form == 1; }
 
 constexpr int kAdjSeg = 16;  // faces per column segment of the batched adjoint flux sweep
 
@@ -1629,6 +1626,12 @@ extern "C" int mfg_reaction_objective(const mfg_box* boxes, int nbox, const mfg_
         rc = MFG_ERR_CUDA;
     cudaFree(d);
     return rc;
+}
+
+extern "C" int mfg_set_adjoint_flux_form(int form) {
+    if (form != 0 && form != 1) return MFG_ERR_ARG;
+    g_adj_flux_form = form;
+    return MFG_OK;
 }
 
 extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_geom* geom, int nsteps, double dt,

@@ -141,14 +141,18 @@ def test_adjoint_rejects_unsupported_configuration():
     assert rc == abi.ERR_STATE
 
 
-def test_flux_sweep_equals_per_face_form(setup, monkeypatch):
+def test_flux_sweep_equals_per_face_form(setup):
     """The column-sweep adjoint flux kernel (default) and its per-face form
     sum the same edge adjoints in a different order: the gradients agree to
     rounding."""
     case, dt, logA, u_in = setup
     ref = ReactionProblem(case, NSTEPS, dt, checkpoint_every=0).gradient(logA, u_in)
-    monkeypatch.setenv("MFG_ADJ_FLUX_PER_FACE", "1")
-    J, gA, gu = ReactionProblem(case, NSTEPS, dt, checkpoint_every=0).gradient(logA, u_in)
+    lib = abi.load()
+    abi.check("form", lib.mfg_set_adjoint_flux_form(0))
+    try:
+        J, gA, gu = ReactionProblem(case, NSTEPS, dt, checkpoint_every=0).gradient(logA, u_in)
+    finally:
+        abi.check("form", lib.mfg_set_adjoint_flux_form(1))
     assert abs(J - ref[0]) <= 1e-13 * abs(ref[0])  # J is an atomic sum
     assert np.allclose(gA, ref[1], rtol=1e-11, atol=1e-13 * np.abs(ref[1]).max())
     assert abs(gu - ref[2]) <= 1e-11 * abs(ref[2]) + 1e-13 * np.abs(ref[1]).max()
