@@ -19,15 +19,17 @@
 // every step.  The volume fraction is a state component, so the RK3 algebra
 // can move it by an ulp (x 1/3 in stage 3), but the geometry does not change.
 // The first call for a box (keyed by its Sborder view and extent) keeps a
-// copy of the grown volume fraction, the list, and every cut cell's
-// fluid-neighbour mask and weights.  Every later call first compares the
-// volume fraction with the copy on the device (exact, bit patterns): the
-// cut-cell kernel uses the stored weights when nothing changed; otherwise it
-// rebuilds the list, recomputes, and (when the new list fits the entry)
-// stores the new weights and volume fraction on the device, so a changed
-// geometry is never served stale weights and no host round trip is needed.
-// All paths give bitwise equal results.  Entries whose new list did not fit
-// are dropped by cutcache_sweep (called where the host synchronizes anyway).
+// copy of the grown volume fraction and the box's cut cells, sorted by their
+// number of fluid neighbours (so the lanes of a warp loop about equally
+// often), with each fluid neighbour's offset and weights laid out so that a
+// warp's loads of one neighbour entry are contiguous.  Every later call first
+// compares the volume fraction with the copy on the device (exact, bit
+// patterns): the cut-cell kernel uses the stored entries when nothing
+// changed; otherwise it rebuilds the list and recomputes on the fly, so a
+// changed geometry is never served stale weights and no host round trip is
+// needed.  All paths give bitwise equal results.  Entries whose volume
+// fraction changed are dropped by cutcache_sweep (called where the host
+// synchronizes anyway) and rebuilt by the next call.
 #include <algorithm>
 #include <unordered_map>
 #include <vector>
@@ -107,70 +109,33 @@ __global__ void cut_vf_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int l1, 
     if (mode == 1 && __any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(dirty, 1u);
 }
 
-__global__ void cut_weights_kernel(CutBox c, const int* __restrict__ list, unsigned n, unsigned long long* mask,
-                                   double* scal, double* wn) {
+__global__ void cut_count_kernel(CutBox c, const int* __restrict__ list, unsigned n, int* __restrict__ kc) {
     const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= n) return;
-    cut_weights_one(c, list[w], (int)w, mask, scal, wn);
+    if (w < n) kc[w] = cut_count_one(c, list[w]);
 }
 
-// Stored weights when the volume fraction is unchanged (*dirty == 0).  Else
-// the freshly built list is processed: when it fits the entry's capacity,
-// each cut cell's weights are stored first (the cache is refreshed on the
-// device, no host round trip) and then applied; otherwise the on-the-fly form
-// runs.  Either way the results are those of the on-the-fly form, bitwise.
+__global__ void cut_entries_kernel(CutBox c, CutCacheView cc, unsigned n, int* off, double* wn, double* wd,
+                                   double* scal) {
+    const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < n) cut_entries_one(c, (int)w, cc, off, wn, wd, scal);
+}
+
+// Stored entries when the volume fraction is unchanged (*dirty == 0), else
+// the on-the-fly form over the freshly built list.  The grid stride is a
+// multiple of 32, so a warp always holds one group of 32 list positions.
 template <int NS>
-__global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, int* __restrict__ clist,
-                                                             const unsigned* __restrict__ ncut, unsigned cap,
-                                                             unsigned long long* mask, double* scal, double* wn,
+__global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, CutCacheView cc, unsigned ncut,
                                                              const unsigned* __restrict__ dirty,
                                                              const int* __restrict__ list,
                                                              const unsigned* __restrict__ count) {
-    const CutCacheView cc = {mask, scal, wn};
     if (*dirty) {
         const unsigned n = *count;
-        const bool refresh = n <= cap;
-        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
-            const int t = list[w];
-            if (refresh) {
-                clist[w] = t;
-                cut_weights_one(c, t, (int)w, mask, scal, wn);
-                cutcell_cached<NS>(c, t, (int)w, cc);
-            } else {
-                cutcell_one<NS>(c, t);
-            }
-        }
+        for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
+            cutcell_one<NS>(c, list[w]);
         return;
     }
-    const unsigned n = *ncut;
-    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x)
-        cutcell_cached<NS>(c, clist[w], (int)w, cc);
-}
-
-// After a refresh: the stored volume fraction and count follow the new
-// geometry and the entry is clean again.  Every block reads *dirty before it
-// counts itself done in ncut[1]; the last block clears the flag.
-__global__ void cut_commit_kernel(Fab S, int lo0, int lo1, int lo2, int l0, int l1, int l2, double* __restrict__ vf,
-                                  unsigned* __restrict__ dirty, const unsigned* __restrict__ count, unsigned cap,
-                                  unsigned* __restrict__ ncut) {
-    if (!*dirty || *count > cap) return;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < (int64_t)l0 * l1 * l2) {
-        int i, j, k;
-        split3(t, l0, l1, i, j, k);
-        vf[t] = S(lo0 + i, lo1 + j, lo2 + k, VFRAC);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned done = atomicAdd(ncut + 1, 1u);
-        if (done == gridDim.x - 1) {
-            ncut[0] = *count;
-            ncut[1] = 0;
-            __threadfence();
-            *dirty = 0;
-        }
-    }
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ncut; w += gridDim.x * blockDim.x)
+        cutcell_cached<NS>(c, (int)w, cc);
 }
 
 double g_wdir_dx[3] = {-1.0, -1.0, -1.0};
@@ -180,13 +145,17 @@ struct CutEntry {
     int64_t js, ks, ns;
     double dx[3];
     double* vf = nullptr;
-    int* list = nullptr;
-    unsigned ncut = 0;            // cut cells when built (capacity of the weight arrays)
-    unsigned* ncut_d = nullptr;   // [current count, commit counter]
-    unsigned long long* mask = nullptr;
-    double* scal = nullptr;
+    int* list = nullptr;          // cut cells, sorted by decreasing fluid-neighbour count
+    int* kc = nullptr;            // fluid-neighbour count by list position
+    int64_t* base = nullptr;      // first entry of each group of 32 list positions
+    int* off = nullptr;           // entries: neighbour offset, weights
     double* wn = nullptr;
+    double* wd = nullptr;
+    double* scal = nullptr;       // 2 per list position
+    unsigned ncut = 0;
     int slot = -1;  // index of this entry's flag in g_cache.dirty
+
+    CutCacheView view() const { return {list, kc, base, off, wn, wd, scal}; }
 };
 
 struct CutCache {
@@ -202,10 +171,12 @@ struct CutCache {
 void free_entry(CutEntry& e) {
     cudaFree(e.vf);
     cudaFree(e.list);
-    cudaFree(e.ncut_d);
-    cudaFree(e.mask);
-    cudaFree(e.scal);
+    cudaFree(e.kc);
+    cudaFree(e.base);
+    cudaFree(e.off);
     cudaFree(e.wn);
+    cudaFree(e.wd);
+    cudaFree(e.scal);
     if (e.slot >= 0) g_cache.free_slots.push_back(e.slot);
     e = CutEntry();
 }
@@ -237,7 +208,9 @@ int new_slot(cudaStream_t st) {
     return g_cache.nslots++;
 }
 
-// Builds the cache entry of a box from its current Sborder (synchronizes once).
+// Builds the cache entry of a box from its current Sborder (synchronizes
+// twice: for the cut-cell list and for the fluid-neighbour counts, which the
+// host sorts).
 bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry& e, cudaStream_t st) {
     const int l0 = c.len[0] + 6, l1 = c.len[1] + 6, l2 = c.len[2] + 6;
     const size_t ng = (size_t)l0 * l1 * l2;
@@ -252,6 +225,7 @@ bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry&
     if (!g_cache.count && cudaMalloc(&g_cache.count, sizeof(unsigned)) != cudaSuccess) return false;
     if (cudaMalloc(&e.vf, ng * sizeof(double)) != cudaSuccess) return false;
     if (cudaMalloc(&e.list, std::max<int64_t>(c.n, 1) * sizeof(int)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.kc, std::max<int64_t>(c.n, 1) * sizeof(int)) != cudaSuccess) return false;
     cut_vf_kernel<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0, l1,
                                                                  l2, e.vf, nullptr, 0);
     cudaMemsetAsync(g_cache.count, 0, sizeof(unsigned), st);
@@ -259,22 +233,50 @@ bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry&
     if (cudaMemcpyAsync(&e.ncut, g_cache.count, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return false;
-    const size_t n = std::max<unsigned>(e.ncut, 1);
-    const size_t need = n * (2 * sizeof(unsigned long long) + 2 * sizeof(double) + CUT_SLOTS * sizeof(double));
+    const unsigned n = e.ncut;
+    std::vector<int> hl(n), hk(n);
+    if (n) {
+        cut_count_kernel<<<(n + TPB - 1) / TPB, TPB, 0, st>>>(c, e.list, n, e.kc);
+        if (cudaMemcpyAsync(hl.data(), e.list, n * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(hk.data(), e.kc, n * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return false;
+    }
+    // decreasing count; equal counts keep the cell order (the compaction's
+    // order varies between runs, so sort equal counts by cell index)
+    std::vector<int> ord(n);
+    for (unsigned w = 0; w < n; ++w) ord[w] = (int)w;
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return hk[x] != hk[y] ? hk[x] > hk[y] : hl[x] < hl[y]; });
+    std::vector<int> sl(n), sk(n);
+    for (unsigned w = 0; w < n; ++w) {
+        sl[w] = hl[ord[w]];
+        sk[w] = hk[ord[w]];
+    }
+    const unsigned ngrp = (n + 31) / 32;
+    std::vector<int64_t> hb(ngrp + 1, 0);
+    for (unsigned gi = 0; gi < ngrp; ++gi) hb[gi + 1] = hb[gi] + 32 * (int64_t)sk[32 * gi];
+    const size_t nent = std::max<int64_t>(hb[ngrp], 1);
+    const size_t need = nent * (sizeof(int) + 2 * sizeof(double)) + (ngrp + 1) * sizeof(int64_t) +
+                        std::max<unsigned>(n, 1) * 2 * sizeof(double);
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || need > fr / 4) return false;  // leave room for the caller
-    if (cudaMalloc(&e.mask, n * 2 * sizeof(unsigned long long)) != cudaSuccess) return false;
-    if (cudaMalloc(&e.scal, n * 2 * sizeof(double)) != cudaSuccess) return false;
-    if (cudaMalloc(&e.wn, n * CUT_SLOTS * sizeof(double)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.base, (ngrp + 1) * sizeof(int64_t)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.off, nent * sizeof(int)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.wn, nent * sizeof(double)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.wd, nent * sizeof(double)) != cudaSuccess) return false;
+    if (cudaMalloc(&e.scal, std::max<unsigned>(n, 1) * 2 * sizeof(double)) != cudaSuccess) return false;
     if ((e.slot = new_slot(st)) < 0) return false;
-    if (cudaMalloc(&e.ncut_d, 2 * sizeof(unsigned)) != cudaSuccess) return false;
-    const unsigned hc[2] = {e.ncut, 0u};
-    if (cudaMemcpyAsync(e.ncut_d, hc, sizeof(hc), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-        return false;
-    if (e.ncut)
-        cut_weights_kernel<<<(e.ncut + TPB - 1) / TPB, TPB, 0, st>>>(c, e.list, e.ncut, e.mask, e.scal, e.wn);
-    g_cache.bytes += ng * sizeof(double) + c.n * sizeof(int) + need;
+    if (n) {
+        if (cudaMemcpyAsync(e.list, sl.data(), n * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(e.kc, sk.data(), n * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(e.base, hb.data(), (ngrp + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st) !=
+                cudaSuccess)
+            return false;
+        cut_entries_kernel<<<(n + TPB - 1) / TPB, TPB, 0, st>>>(c, e.view(), n, e.off, e.wn, e.wd, e.scal);
+        // the host vectors above are read by the copies: wait for them
+        if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+    }
+    g_cache.bytes += ng * sizeof(double) + 2 * c.n * sizeof(int) + need;
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -375,17 +377,13 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
                                                                       l1, l2, ce->vf, dirty, 1);
         cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, dirty);
         const unsigned ng = (unsigned)std::min<int64_t>(std::max<int64_t>(nb, 1), 152 * 8);
-        const unsigned cap = ce->ncut;
-#define MFG_CUT_ARGS c, ce->list, ce->ncut_d, cap, ce->mask, ce->scal, ce->wn, dirty, list, count
+#define MFG_CUT_ARGS c, ce->view(), ce->ncut, dirty, list, count
         if (ns <= 1) cutcell_cached_kernel<1><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
         else if (ns <= 2) cutcell_cached_kernel<2><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
         else if (ns <= 4) cutcell_cached_kernel<4><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
         else if (ns <= 8) cutcell_cached_kernel<8><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
         else cutcell_cached_kernel<16><<<ng, TPB, 0, st>>>(MFG_CUT_ARGS);
 #undef MFG_CUT_ARGS
-        cut_commit_kernel<<<(unsigned)((ngc + 255) / 256), 256, 0, st>>>(c.S, b.lo[0] - 3, b.lo[1] - 3, b.lo[2] - 3, l0,
-                                                                          l1, l2, ce->vf, dirty, count, cap,
-                                                                          ce->ncut_d);
         return cudaGetLastError();
     }
     cut_list_kernel<<<nb, TPB, 0, st>>>(c, list, count, nullptr);

@@ -3,10 +3,11 @@
 // (mfg_ib.cu) and the batched launches over all boxes (mfg_batch.cu).
 //
 // Two forms of the same arithmetic: cutcell_one computes the inverse-distance
-// weights of the 5^3 neighbourhood on the fly; cut_weights_one stores them
-// (fluid-neighbour mask, 1/den, 1/sum w, the 125 weights) and cutcell_cached
-// applies stored weights.  Both accumulate in the same neighbour order and
-// finish with the same multiplications, so they give bitwise equal results.
+// weights of the 5^3 neighbourhood on the fly; cut_entries_one stores, for
+// each fluid neighbour in neighbourhood order, its offset and both weights
+// (plus 1/den and 1/sum w per cut cell) and cutcell_cached applies them.
+// Both accumulate in the same neighbour order and finish with the same
+// multiplications, so they give bitwise equal results.
 #pragma once
 #include "mfg_internal.h"
 #include "mfg_physics.cuh"
@@ -20,7 +21,7 @@ namespace {
 
 constexpr int SG = 2;  // STENCILGROW
 constexpr int SW = 2 * SG + 1;
-constexpr int CUT_SLOTS = 128;  // stored weights per cut cell (125 used)
+constexpr int CUT_BATCH = 4;  // neighbour entries whose gathers are issued together
 
 
 struct CutBox {
@@ -32,11 +33,18 @@ struct CutBox {
     double* tcht;  // conjugate-heat-transfer temperature average per valid cell (or null)
 };
 
-// Stored weights of the cut cells of one box (list position w).
+// Stored entries of the cut cells of one box.  Cut cells sit in the list in
+// decreasing order of their fluid-neighbour count, so the 32 cells of a warp
+// loop about as often; entry e of list position w lives at
+// base[w / 32] + 32 e + w % 32, so a warp's loads of entry e are contiguous.
 struct CutCacheView {
-    const unsigned long long* mask;  // 2 per cut cell: fluid-neighbour bits by slot
-    const double* scal;              // 2 per cut cell: 1/den of the velocity weights (0: zero velocity), 1/sum w
-    const double* wn;                // CUT_SLOTS per cut cell: IDW weight by slot
+    const int* list;       // cell index by list position
+    const int* kc;         // fluid neighbours by list position
+    const int64_t* base;   // first entry of each group of 32 list positions
+    const int* off;        // offset of the neighbour from the cell in Sborder
+    const double* wn;      // inverse-distance weight about the surface point
+    const double* wd;      // Dirichlet velocity weight
+    const double* scal;    // 2 per list position: 1/den (0: zero velocity), 1/sum wn
 };
 
 __device__ __forceinline__ void cell_of(const CutBox& c, int64_t t, int& i, int& j, int& k) {
@@ -174,82 +182,122 @@ __device__ __forceinline__ void cutcell_one(const CutBox& c, int64_t t) {
     cut_finish<NS>(c, t, o, vel_iden(c, dist, swd), have, have ? 1.0 / swn : 0.0, sv, sp, st, sr, ss);
 }
 
-// Stores the weights of cut cell t of the box at list position w.
-__device__ __forceinline__ void cut_weights_one(const CutBox& c, int64_t t, int w, unsigned long long* mask,
-                                                double* scal, double* wnp) {
+// Number of vfrac == 1 cells in the 5^3 neighbourhood of cut cell t.
+__device__ __forceinline__ int cut_count_one(const CutBox& c, int64_t t) {
     int i, j, k;
     cell_of(c, t, i, j, k);
     const Fab& S = c.S;
     const int64_t o = S.off(i, j, k);
     const double* V = S.p + VFRAC * S.ns;
+    int cnt = 0;
+    for (int n = -SG; n <= SG; ++n)
+        for (int m = -SG; m <= SG; ++m)
+            for (int l = -SG; l <= SG; ++l) cnt += is_one(V[o + l + m * S.js + n * S.ks]) ? 1 : 0;
+    return cnt;
+}
+
+// Stores the entries of the cut cell at list position w (cell cc.list[w]).
+__device__ __forceinline__ void cut_entries_one(const CutBox& c, int w, const CutCacheView& cc, int* offp,
+                                                double* wnp, double* wdp, double* scal) {
+    int i, j, k;
+    cell_of(c, cc.list[w], i, j, k);
+    const Fab& S = c.S;
+    const int64_t o = S.off(i, j, k);
+    const double* V = S.p + VFRAC * S.ns;
     double dist, xpn[3], dxnd[3];
     cut_geometry(c, o, dist, xpn, dxnd);
-    unsigned long long m0 = 0, m1 = 0;
     double swd = 0.0, swn = 0.0;
-    double* W = wnp + (int64_t)w * CUT_SLOTS;
+    int64_t ix = cc.base[w >> 5] + (w & 31);
     for (int n = -SG; n <= SG; ++n)
         for (int m = -SG; m <= SG; ++m)
             for (int l = -SG; l <= SG; ++l) {
-                const int64_t q = o + l + m * S.js + n * S.ks;
-                if (!is_one(V[q])) continue;
+                const int64_t q = l + m * S.js + n * S.ks;
+                if (!is_one(V[o + q])) continue;
                 const int slot = (l + SG) + SW * ((m + SG) + SW * (n + SG));
-                if (slot < 64)
-                    m0 |= 1ull << slot;
-                else
-                    m1 |= 1ull << (slot - 64);
-                if (!(l == 0 && m == 0 && n == 0)) swd += c_wdir[slot];
+                const bool centre = l == 0 && m == 0 && n == 0;
+                if (!centre) swd += c_wdir[slot];
                 const double a = l * dxnd[0] - xpn[0], b = m * dxnd[1] - xpn[1], e = n * dxnd[2] - xpn[2];
                 const double wn = rcp_pos(((a * a + b * b) + e * e) + kTiny2);
-                W[slot] = wn;
+                offp[ix] = (int)q;
+                wnp[ix] = wn;
+                wdp[ix] = centre ? 0.0 : c_wdir[slot];
+                ix += 32;
                 swn += wn;
             }
-    mask[2 * (int64_t)w] = m0;
-    mask[2 * (int64_t)w + 1] = m1;
     scal[2 * (int64_t)w] = vel_iden(c, dist, swd);
     scal[2 * (int64_t)w + 1] = swn > 0.0 ? 1.0 / swn : 0.0;
 }
 
-// Cached form: the stored weights applied in the on-the-fly order.
+// Cached form: the stored entries applied in the on-the-fly order.  A cut
+// cell is never its own fluid neighbour (its vfrac is below one), so every
+// entry carries a velocity weight, as in the on-the-fly loop.
 template <int NS>
-__device__ __forceinline__ void cutcell_cached(const CutBox& c, int64_t t, int w, const CutCacheView& cc) {
+__device__ __forceinline__ void cutcell_cached(const CutBox& c, int w, const CutCacheView& cc) {
+    const int64_t t = cc.list[w];
     int i, j, k;
     cell_of(c, t, i, j, k);
     const Fab& S = c.S;
     const int64_t o = S.off(i, j, k);
     const DevParams& P = c_P;
     const bool interp_spec = !P.species_in_solid;
-    const double* W = cc.wn + (int64_t)w * CUT_SLOTS;
     double sv[3] = {0.0, 0.0, 0.0};
     double sp = 0.0, st = 0.0, sr = 0.0, ss[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) ss[s] = 0.0;
-    const unsigned long long mk[2] = {cc.mask[2 * (int64_t)w], cc.mask[2 * (int64_t)w + 1]};
-    for (int h = 0; h < 2; ++h) {
-        unsigned long long bits = mk[h];
-        while (bits) {
-            const int slot = h * 64 + __ffsll((long long)bits) - 1;
-            bits &= bits - 1;
-            const int l = slot % SW - SG, m = (slot / SW) % SW - SG, n = slot / (SW * SW) - SG;
-            const int64_t q = o + l + m * S.js + n * S.ks;
-            if (slot != (SW * SW * SW) / 2) {
-                const double wd = c_wdir[slot];
-                sv[0] += S.p[q + VELX * S.ns] * wd;
-                sv[1] += S.p[q + VELY * S.ns] * wd;
-                sv[2] += S.p[q + VELZ * S.ns] * wd;
-            }
-            const double wn = W[slot];
-            sp += S.p[q + PRES * S.ns] * wn;
-            st += S.p[q + TEMP * S.ns] * wn;
-            sr += S.p[q + DENS * S.ns] * wn;
+    const int kn = cc.kc[w];
+    int64_t ix = cc.base[w >> 5] + (w & 31);
+    // batches of CUT_BATCH entries: all gathers of a batch are issued before
+    // its sums, which then run in neighbour order
+    int e = 0;
+    for (; e + CUT_BATCH <= kn; e += CUT_BATCH, ix += 32 * CUT_BATCH) {
+        int64_t q[CUT_BATCH];
+        double wd[CUT_BATCH], wn[CUT_BATCH], v[CUT_BATCH][6];
+#pragma unroll
+        for (int u = 0; u < CUT_BATCH; ++u) {
+            q[u] = o + cc.off[ix + 32 * u];
+            wd[u] = cc.wd[ix + 32 * u];
+            wn[u] = cc.wn[ix + 32 * u];
+        }
+#pragma unroll
+        for (int u = 0; u < CUT_BATCH; ++u) {
+            v[u][0] = S.p[q[u] + VELX * S.ns];
+            v[u][1] = S.p[q[u] + VELY * S.ns];
+            v[u][2] = S.p[q[u] + VELZ * S.ns];
+            v[u][3] = S.p[q[u] + PRES * S.ns];
+            v[u][4] = S.p[q[u] + TEMP * S.ns];
+            v[u][5] = S.p[q[u] + DENS * S.ns];
+        }
+#pragma unroll
+        for (int u = 0; u < CUT_BATCH; ++u) {
+            sv[0] += v[u][0] * wd[u];
+            sv[1] += v[u][1] * wd[u];
+            sv[2] += v[u][2] * wd[u];
+            sp += v[u][3] * wn[u];
+            st += v[u][4] * wn[u];
+            sr += v[u][5] * wn[u];
             if (interp_spec) {
 #pragma unroll
                 for (int s = 0; s < NS; ++s)
-                    if (s < P.nspec) ss[s] += S.p[q + (NFLO + s) * S.ns] * wn;
+                    if (s < P.nspec) ss[s] += S.p[q[u] + (NFLO + s) * S.ns] * wn[u];
             }
         }
     }
-    const bool have = (mk[0] | mk[1]) != 0;
-    cut_finish<NS>(c, t, o, cc.scal[2 * (int64_t)w], have, cc.scal[2 * (int64_t)w + 1], sv, sp, st, sr, ss);
+    for (; e < kn; ++e, ix += 32) {
+        const int64_t q = o + cc.off[ix];
+        const double wd = cc.wd[ix], wn = cc.wn[ix];
+        sv[0] += S.p[q + VELX * S.ns] * wd;
+        sv[1] += S.p[q + VELY * S.ns] * wd;
+        sv[2] += S.p[q + VELZ * S.ns] * wd;
+        sp += S.p[q + PRES * S.ns] * wn;
+        st += S.p[q + TEMP * S.ns] * wn;
+        sr += S.p[q + DENS * S.ns] * wn;
+        if (interp_spec) {
+#pragma unroll
+            for (int s = 0; s < NS; ++s)
+                if (s < P.nspec) ss[s] += S.p[q + (NFLO + s) * S.ns] * wn;
+        }
+    }
+    cut_finish<NS>(c, t, o, cc.scal[2 * (int64_t)w], kn > 0, cc.scal[2 * (int64_t)w + 1], sv, sp, st, sr, ss);
 }
 
 }  // namespace
