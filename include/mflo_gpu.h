@@ -299,12 +299,21 @@ int mfg_set_weno_mode(int fast);
  * fraction only, which the solver never changes; update_cutcells
  * (ib_utils.H:272-436) recomputes them every stage.  With the cache on
  * (default) the first mfg_cutcells / mfg_advance_level call for a box keeps
- * them in device memory (synchronizes once; about 1 KiB per cut cell), and
+ * them in device memory (synchronizes twice; 24 B per cut cell plus 20 B per
+ * fluid neighbour, about 0.3 KiB per cut cell in a sphere pack), and
  * every later call checks the box's grown volume fraction against a stored
  * copy on the device (exact) before using them: a changed geometry falls back
  * to recomputation in the same call and is dropped from the cache.  Results
  * are bitwise the same either way.  enable = 0 frees the cache.  Synchronizes. */
 int mfg_set_cutcell_cache(int enable);
+
+/* Form of the face pass of orders 1 and 2 with Navier-Stokes terms
+ * (compute_flux, compute_flux_3d.H:88-430, whose faces on the solid side,
+ * face vfrac < 1/2, carry conduction and diffusion only): 1 (default) writes
+ * those faces in one pass and runs the flux branch over a compacted list of
+ * the others, 0 runs every face in one kernel.  Bitwise the same results.
+ * Synchronizes. */
+int mfg_set_face_compaction(int on);
 
 /* Integrator of the chemistry sub-step (mfg_chem_substep, mfg_advance_level,
  * the box-list steps): kind 0 (default) the explicit SSP-RK3 of the

@@ -101,6 +101,7 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), _VP]),
     ("mfg_set_weno_mode", C.c_int, [C.c_int]),
     ("mfg_set_cutcell_cache", C.c_int, [C.c_int]),
+    ("mfg_set_face_compaction", C.c_int, [C.c_int]),
     ("mfg_profile", C.c_int, [C.c_int]),
     ("mfg_profile_read", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
     ("mfg_profile_name", C.c_char_p, [C.c_int]),

@@ -94,7 +94,7 @@ int cuda_rc(cudaError_t e) {
 size_t rhs_scratch_doubles(const int n[3]) {
     size_t s = aux_doubles(n);
     for (int d = 0; d < 3; ++d) s += face_doubles(n, d, NFS) + face_doubles(n, d, ncomp_adv());
-    return s;
+    return s + face_list_doubles(n);
 }
 
 // Lay out one box's RHS scratch at base.
@@ -127,6 +127,8 @@ RhsBox make_rhs_box(const mfg_box& b, const mfg_geom& g, double* base) {
         B.flx[d] = dense_fab(p, b.lo, len);
         p += face_doubles(n, d, ncomp_adv());
     }
+    B.fcount = reinterpret_cast<unsigned*>(p);
+    B.flist = reinterpret_cast<int*>(p) + 4;
     return B;
 }
 

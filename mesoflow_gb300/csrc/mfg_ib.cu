@@ -365,7 +365,7 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
     const int ns = c_host_params().nspec;
     CutEntry* ce = find_entry(b, c, g, st);
-    ProfScope ps(K_CUT, st);
+    ProfScope ps(K_CUT, st, (ce ? 3 : 2) + (c_host_params().conj_ht ? 1 : 0));
     if (c_host_params().conj_ht) cht_avg_kernel<<<nb, TPB, 0, st>>>(c);
     cudaMemsetAsync(count, 0, sizeof(unsigned), st);
     if (ce) {

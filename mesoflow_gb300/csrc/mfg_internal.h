@@ -36,9 +36,11 @@ enum KernelKind {
 // True while mfg_profile is on (per-launch CUDA events are recorded).
 bool profile_enabled();
 
+// Counts the kernels launched inside it (nlaunch) and, while profiling is
+// on, times them as one entry of their kind.
 class ProfScope {
   public:
-    ProfScope(int kind, cudaStream_t st);
+    ProfScope(int kind, cudaStream_t st, int nlaunch = 1);
     ~ProfScope();
 
   private:
@@ -57,6 +59,9 @@ struct RhsBox {
     Fab aux;
     Fab fs[3];
     Fab flx[3];
+    int* flist;        // active faces of the three directions, one after the other (orders 1, 2
+                       // with Navier-Stokes terms)
+    unsigned* fcount;  // 3: active faces per direction
 };
 
 const DevParams& c_host_params();
@@ -81,6 +86,12 @@ inline size_t aux_doubles(const int n[3]) {
 }
 inline size_t face_doubles(const int n[3], int d, int ncomp) {
     return (size_t)(n[0] + (d == 0)) * (n[1] + (d == 1)) * (n[2] + (d == 2)) * ncomp;
+}
+// Four counters and the active-face lists of the three directions, as doubles.
+inline size_t face_list_doubles(const int n[3]) {
+    size_t m = 0;
+    for (int d = 0; d < 3; ++d) m += face_doubles(n, d, 1);
+    return (m + 4 + 1) / 2;
 }
 
 // Other kernels (mfg_ib.cu, mfg_fill.cu, mfg_step.cu)

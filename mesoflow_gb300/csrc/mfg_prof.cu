@@ -52,8 +52,8 @@ void drain() {
 
 bool profile_enabled() { return g_on; }
 
-ProfScope::ProfScope(int kind, cudaStream_t st) : kind_(kind), st_(st), a_(nullptr) {
-    ++g_launches;
+ProfScope::ProfScope(int kind, cudaStream_t st, int nlaunch) : kind_(kind), st_(st), a_(nullptr) {
+    g_launches += (unsigned long long)nlaunch;
     if (g_on) {
         a_ = ev();
         cudaEventRecord((cudaEvent_t)a_, st_);

@@ -7,7 +7,12 @@
 //                 inside every face's geteulerflux / get_max_eigenvalue).
 //   face_kernel   per face of growHi(bx,d,1): scheme scalars (LLF eigenvalue,
 //                 AUSM+-up Mach/pressure terms), IB flags, viscous stress and
-//                 heat-conduction terms.
+//                 heat-conduction terms.  Orders 1/2 with Navier-Stokes terms
+//                 split it: face_split_kernel writes the faces on the solid
+//                 side (conduction and diffusion only) and lists the others,
+//                 face_list_kernel runs the flux branch over those lists, each
+//                 for the three directions in one launch, so no lane of a warp
+//                 idles on a solid-side face.
 //   flux_kernel   per (face, component): the hyperbolic flux of one
 //                 component (WENO5-JS / MUSCL+AUSM+-up / central), species
 //                 diffusion, and the viscous terms, written once per face and
@@ -34,6 +39,7 @@ __device__ unsigned int g_status = 0;
 namespace {
 
 constexpr int TPB = 256;
+bool g_face_split = true;  // mfg_set_face_compaction
 
 template <int NS>
 __global__ void __launch_bounds__(TPB) prim_kernel(RhsBox B) {
@@ -42,6 +48,43 @@ __global__ void __launch_bounds__(TPB) prim_kernel(RhsBox B) {
 template <int NS>
 __global__ void __launch_bounds__(TPB) face_kernel(RhsBox B, int d) {
     face_body<NS>(B, d, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+}
+// Orders 1 and 2 with Navier-Stokes terms: the inactive faces (solid side,
+// conduction and diffusion only) of all three directions are written here
+// (blockIdx.y = direction) and the active ones listed per direction (one
+// atomic per warp), so that face_list_kernel runs the flux branch of all
+// three directions in one launch with every lane of a warp busy (blocks past
+// a direction's count exit at once).  Same
+// per-face arithmetic: bitwise the results of face_kernel.
+__device__ __forceinline__ int64_t face_list_off(const RhsBox& B, int d) {
+    int64_t o = 0;
+    for (int e = 0; e < d; ++e) o += face_count(B, e);
+    return o;
+}
+template <int NS>
+__global__ void __launch_bounds__(TPB) face_split_kernel(RhsBox B) {
+    const int d = blockIdx.y;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = false;
+    if (t < face_count(B, d)) {
+        act = face_active(B, d, t);
+        if (!act) face_body<NS>(B, d, t);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    unsigned base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(B.fcount + d, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    if (act) B.flist[face_list_off(B, d) + base + __popc(m & ((1u << lane) - 1u))] = (int)t;
+}
+// The direction is the block's (blockIdx.y), uniform as in face_kernel, so
+// the compiler forms the same multiply-adds in both.
+template <int NS>
+__global__ void __launch_bounds__(TPB) face_list_kernel(RhsBox B) {
+    const int d = blockIdx.y;
+    const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < B.fcount[d]) face_body<NS>(B, d, B.flist[face_list_off(B, d) + w]);
 }
 template <bool FAST>
 __global__ void __launch_bounds__(TPB) flux_kernel(RhsBox B, int d) {
@@ -79,14 +122,27 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
         ProfScope ps(K_PRIM, st);
         prim_kernel<NS><<<blocks_for(ng), TPB, 0, st>>>(B);
     }
-    for (int d = 0; d < 3; ++d) {
+    const bool split = g_face_split && c_host_params().do_ns && ord <= 2;
+    if (split) {
+        int64_t nfmax = 0;
+        for (int d = 0; d < 3; ++d) {
+            int64_t nf = 1;
+            for (int e = 0; e < 3; ++e) nf *= (B.hi[e] - B.lo[e] + 1 + (e == d));
+            nfmax = std::max(nfmax, nf);
+        }
+        cudaMemsetAsync(B.fcount, 0, 3 * sizeof(unsigned), st);
+        ProfScope ps(K_FACE, st, 2);
+        face_split_kernel<NS><<<dim3(blocks_for(nfmax), 3), TPB, 0, st>>>(B);
+        face_list_kernel<NS><<<dim3(blocks_for(nfmax), 3), TPB, 0, st>>>(B);
+    }
+    for (int d = 0; d < 3 && !split; ++d) {
         int64_t nf = 1;
         for (int e = 0; e < 3; ++e) nf *= (B.hi[e] - B.lo[e] + 1 + (e == d));
         {
             ProfScope ps(K_FACE, st);
             face_kernel<NS><<<blocks_for(nf), TPB, 0, st>>>(B, d);
         }
-        if (c_host_params().do_ns && ord <= 2) continue;  // the face kernel wrote the fluxes
+        if (c_host_params().do_ns && ord <= 2) continue;  // the face kernels wrote the fluxes
         ProfScope ps(K_FLUX, st);
         if (fast && ord == 5 && c_host_params().do_ns) {
             int seg = 32;
@@ -136,3 +192,9 @@ cudaError_t launch_rhs_box(const RhsBox& B, int stage, double dt, bool fast, cud
 }
 
 }  // namespace mfg
+
+extern "C" int mfg_set_face_compaction(int on) {
+    if (cudaDeviceSynchronize() != cudaSuccess) return MFG_ERR_CUDA;
+    mfg::g_face_split = on != 0;
+    return MFG_OK;
+}

@@ -168,6 +168,28 @@ __device__ __forceinline__ void prim_body(const RhsBox& B, int64_t t) {
 // ---------------------------------------------------------------------------
 // face_kernel: per-face scalars for direction d
 // ---------------------------------------------------------------------------
+// Faces of direction d (growHi(bx, d, 1)).
+__device__ __forceinline__ int64_t face_count(const RhsBox& B, int d) {
+    int64_t nf = 1;
+    for (int e = 0; e < 3; ++e) nf *= B.hi[e] - B.lo[e] + 1 + (e == d);
+    return nf;
+}
+
+// Whether face t of direction d takes the flux branch of face_body
+// (Navier-Stokes terms on and face volume fraction >= 1/2), by the same
+// arithmetic.
+__device__ __forceinline__ bool face_active(const RhsBox& B, int d, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    const Idx3 f = delinear(t, lo, len);
+    const Fab& S = B.sb;
+    const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
+    const int64_t oR = S.off(f.i, f.j, f.k);
+    const double* vf = S.p + VFRAC * S.ns;
+    const double facevfrac = 0.5 * (vf[oR - sd] + vf[oR]);
+    return c_P.do_ns && nonneg_ge(facevfrac, 0.5);
+}
+
 template <int NS>
 __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
     int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];

@@ -185,7 +185,7 @@ cudaError_t launch_resnorm_box(const mfg_box& b, double dt, double* partial, dou
     // 16 cells per thread: blocks of one cell per thread were dominated by their fixed cost
     int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + 16 * TPB - 1) / (16 * TPB)));
     dim3 g(nblk, nc);
-    ProfScope ps(K_RESNORM, st);
+    ProfScope ps(K_RESNORM, st, 2);
     resnorm_kernel<<<g, TPB, 0, st>>>(v, make_fab(b.s_new), make_fab(b.s_old), 1.0 / dt, -1.0 / dt, partial, nblk);
     resnorm_final_kernel<<<nc, 32, 0, st>>>(partial, nblk, acc);
     return cudaGetLastError();
