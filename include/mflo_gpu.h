@@ -502,6 +502,13 @@ unsigned long long mfg_launch_count(void);
  * kernels.  Allocates a small buffer.  Synchronizes. */
 int mfg_measure_fp64_peak(double* tflops, void* stream);
 
+/* Self-test of the integer-pipe form of x + 0.0 that the stage update uses
+ * (the sum of a state value and a rate of exactly +0): compares it bit for
+ * bit with the FP64 add on n values (boundary values, then pseudo-random bit
+ * patterns; NaN skipped) and returns the number of mismatches.
+ * Synchronizes. */
+int mfg_selftest_exact_ops(unsigned long long n, unsigned* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

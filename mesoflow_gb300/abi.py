@@ -108,6 +108,7 @@ SIGNATURES = [
     ("mfg_launch_count", C.c_ulonglong, []),
     ("mfg_compute_dsdt_flow_noalloc", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, _VP]),
     ("mfg_measure_fp64_peak", C.c_int, [C.POINTER(C.c_double), _VP]),
+    ("mfg_selftest_exact_ops", C.c_int, [C.c_ulonglong, C.POINTER(C.c_uint)]),
     ("mfg_boxlist_create", C.c_int, [_BP, C.c_int, _GP, C.c_int, C.POINTER(C.c_void_p)]),
     ("mfg_boxlist_destroy", C.c_int, [C.c_void_p]),
     ("mfg_boxlist_step", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _VP]),

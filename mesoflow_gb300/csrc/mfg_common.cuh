@@ -110,6 +110,15 @@ __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, 
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 
+// x + 0.0 without the FP64 pipe: -0 becomes +0, anything else is x (a NaN
+// keeps its bits, where the add would quiet a signalling NaN; the states
+// never hold one and a NaN rate raises MFG_STATUS_NAN).
+__device__ __forceinline__ bool is_zero_bits(double x) { return (__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ double plus_zero(double x) { return is_zero_bits(x) ? 0.0 : x; }
+__device__ __forceinline__ bool is_finite_bits(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // Volume-fraction tests on the integer pipe: for v >= 0 the IEEE order of
 // doubles is the order of their bit patterns, so v < 1 and v == 1 need no
 // FP64 compare (the FP64 pipe is the bottleneck of these kernels).

@@ -116,8 +116,48 @@ __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
     for (int q = 0; q < 8; ++q) s += x[q];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+
+// Checks plus_zero (x + 0.0 on the integer pipe, used by the stage update)
+// against the FP64 add, bit for bit, on boundary values (zeros, subnormals,
+// the normal range's ends, infinities) and on pseudo-random bit patterns
+// (xorshift64); NaN operands are skipped.  Counts mismatches in *bad.
+__device__ unsigned long long exact_ops_value(unsigned long long i) {
+    const unsigned long long special[] = {
+        0x0000000000000000ULL, 0x0000000000000001ULL, 0x000FFFFFFFFFFFFFULL, 0x0010000000000000ULL,
+        0x0020000000000000ULL, 0x0030000000000000ULL, 0x0031234567890ABCULL, 0x3FD0000000000000ULL,
+        0x3FF0000000000000ULL, 0x7FD0000000000000ULL, 0x7FDFFFFFFFFFFFFFULL, 0x7FE0000000000000ULL,
+        0x7FEFFFFFFFFFFFFFULL, 0x7FF0000000000000ULL, 0x0008000000000000ULL, 0x001FFFFFFFFFFFFFULL};
+    const unsigned ns = sizeof(special) / sizeof(special[0]);
+    if (i < 2 * ns) return special[i % ns] | ((i >= ns) ? 0x8000000000000000ULL : 0ULL);
+    unsigned long long x = i * 0x9E3779B97F4A7C15ULL + 0x2545F4914F6CDD1DULL;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return x;
+}
+__device__ bool is_nan_bits(unsigned long long b) { return ((b >> 52) & 0x7ff) == 0x7ff && (b << 12) != 0; }
+__global__ void exact_ops_kernel(unsigned long long n, unsigned* bad) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long bx = exact_ops_value(i);
+    if (is_nan_bits(bx)) return;
+    const double x = __longlong_as_double(bx);
+    const unsigned m = __double_as_longlong(plus_zero(x)) != __double_as_longlong(__dadd_rn(x, 0.0)) ? 1u : 0u;
+    if (m) atomicAdd(bad, m);
+}
 }  // namespace
 }  // namespace mfg
+
+extern "C" int mfg_selftest_exact_ops(unsigned long long n, unsigned* mismatches) {
+    if (!mismatches || n == 0 || n > (1ULL << 32)) return MFG_ERR_ARG;
+    unsigned* d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned)) != cudaSuccess) return MFG_ERR_CUDA;
+    cudaMemset(d, 0, sizeof(unsigned));
+    mfg::exact_ops_kernel<<<(unsigned)((n + 255) / 256), 256>>>(n, d);
+    const cudaError_t e = cudaMemcpy(mismatches, d, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return (e == cudaSuccess && cudaGetLastError() == cudaSuccess) ? MFG_OK : MFG_ERR_CUDA;
+}
 
 extern "C" int mfg_measure_fp64_peak(double* tflops, void* stream) {
     if (!tflops) return MFG_ERR_ARG;

@@ -532,8 +532,28 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
     if (t >= nc) return;  // n: state component
     const Idx3 x = delinear(t, lo, len);
     const DevParams& P = c_P;
-    double ds = 0.0;
     const bool advected = (n < NCONS) || (n >= NFLO);
+    if (!advected && is_finite_bits(dt) && __double_as_longlong(dt) >= 0) {
+        // A component without a flux (velocities, pressure, temperature,
+        // density, vfrac) has the rate +0 exactly, so for a finite dt >= +0
+        // dt * ds = +0 and v + dt * ds = v + 0 (plus_zero): the same bits
+        // without the two FP64 operations.  n and dt are uniform over a block, so this is a branch
+        // of whole warps, not a predicated path.
+        if (B.dsdt.p) B.dsdt(x.i, x.j, x.k, n) = 0.0;
+        if (stage == 1) {
+            B.snew(x.i, x.j, x.k, n) = plus_zero(B.sb(x.i, x.j, x.k, n));
+        } else if (stage == 2) {
+            double v = plus_zero(B.snew(x.i, x.j, x.k, n));
+            v = add(v, mul(3.0, B.sold(x.i, x.j, x.k, n)));
+            B.snew(x.i, x.j, x.k, n) = mul(v, 0.25);
+        } else if (stage == 3) {
+            double v = plus_zero(B.snew(x.i, x.j, x.k, n));
+            v = add(B.sold(x.i, x.j, x.k, n), mul(2.0, v));
+            B.snew(x.i, x.j, x.k, n) = mul(v, kThird);
+        }
+        return;
+    }
+    double ds = 0.0;
     if (advected) {
         const int c = (n < NCONS) ? n : n - (NFLO - NCONS);
         const Fab &Fx = B.flx[0], &Fy = B.flx[1], &Fz = B.flx[2];
@@ -542,7 +562,7 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
         const int64_t oz = Fz.off(x.i, x.j, x.k) + c * Fz.ns;
         ds = ((Fx.p[ox] - Fx.p[ox + 1]) * B.idx[0] + (Fy.p[oy] - Fy.p[oy + Fy.js]) * B.idx[1]) +
              (Fz.p[oz] - Fz.p[oz + Fz.ks]) * B.idx[2];
-        ds = ds + 0.0;  // + source (compute_fluid_source is zero)
+        ds = plus_zero(ds);  // + source (compute_fluid_source is zero)
     }
     const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
     const int nnull = (P.species_in_solid == 1) ? NFLO : NFLO + P.nspec;
