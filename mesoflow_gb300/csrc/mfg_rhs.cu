@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(TPB) face_split_kernel(RhsBox B) {
     bool act = false;
     if (t < face_count(B, d)) {
         act = face_active(B, d, t);
-        if (!act) face_body<NS>(B, d, t);
+        if (!act) face_body<NS, true>(B, d, t);
     }
     const unsigned m = __ballot_sync(0xffffffffu, act);
     if (!m) return;

@@ -190,7 +190,9 @@ __device__ __forceinline__ bool face_active(const RhsBox& B, int d, int64_t t) {
     return c_P.do_ns && nonneg_ge(facevfrac, 0.5);
 }
 
-template <int NS>
+// SOLID_SIDE: the caller knows the face is not active (face_split_kernel);
+// the flux branch is compiled out and the remaining arithmetic is the same.
+template <int NS, bool SOLID_SIDE = false>
 __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
     int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
     for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
@@ -211,7 +213,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
 #pragma unroll
     for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
     const double facevfrac = 0.5 * (vf[oL] + vf[oR]);
-    const bool active = P.do_ns && nonneg_ge(facevfrac, 0.5);
+    const bool active = !SOLID_SIDE && P.do_ns && nonneg_ge(facevfrac, 0.5);
 
     double fs[NFS];
 #pragma unroll
