@@ -6,6 +6,10 @@
 // along d*: the highest direction of D whose boundary is ext_dir (the user
 // functor runs after the extrapolation rules and checks x, y, z in turn,
 // Source/mflo_bcfill.H:236-320), otherwise the highest direction of D.
+// The physical-boundary launches cover only the blocks ("slabs") of the
+// grown boxes that lie outside the domain, listed once per box layout, not
+// every grown cell of every box.
+#include <algorithm>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -27,6 +31,13 @@ struct FillGeom {
     int gran;       // owner-map granularity (cells)
     int mlen[3];    // owner-map extent
     double dx[3], plo[3];
+};
+
+// A block of a box's grown region outside the domain: its cells leave the
+// domain through the same directions (the bc_kernel stage = their number).
+struct BcSlab {
+    int box;
+    int lo[3], len[3];
 };
 
 __device__ __forceinline__ void grown_cell(const FillBox& b, int64_t t, int& i, int& j, int& k, int64_t& n) {
@@ -66,14 +77,19 @@ __global__ void copy_kernel(const FillBox* __restrict__ boxes, FillGeom G, const
     for (int c = 0; c < ncomp; ++c) b.sb.p[qd + c * b.sb.ns] = o.src.p[qs + c * o.src.ns];
 }
 
+// One launch per stage over the slabs of that stage only (blockIdx.y = slab).
 template <int NS>
-__global__ void bc_kernel(const FillBox* __restrict__ boxes, FillGeom G, int stage, int ncomp) {
-    const FillBox& b = boxes[blockIdx.y];
-    int i, j, k;
-    int64_t n;
+__global__ void bc_kernel(const FillBox* __restrict__ boxes, const BcSlab* __restrict__ slabs, FillGeom G, int stage,
+                          int ncomp) {
+    const BcSlab& sl = slabs[blockIdx.y];
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    grown_cell(b, t, i, j, k, n);
-    if (t >= n) return;
+    if (t >= (int64_t)sl.len[0] * sl.len[1] * sl.len[2]) return;
+    const FillBox& b = boxes[sl.box];
+    int i, j, k;
+    split3(t, sl.len[0], sl.len[1], i, j, k);
+    i += sl.lo[0];
+    j += sl.lo[1];
+    k += sl.lo[2];
     const int iv[3] = {i, j, k};
     bool out[3];
     int nout = 0;
@@ -128,6 +144,10 @@ struct OwnerCache {
     FillBox* d_boxes = nullptr;
     size_t bcap = 0;
     std::vector<char> table;
+    BcSlab* d_slabs = nullptr;  // grouped by stage 1, 2, 3
+    size_t scap = 0;
+    int nslab[3] = {0, 0, 0}, soff[3] = {0, 0, 0};
+    int64_t smax[3] = {0, 0, 0};  // largest slab of each stage (cells)
 } g_fill;
 
 int igcd(int a, int b) {
@@ -148,6 +168,7 @@ cudaError_t ensure_owner(const mfg_box* boxes, int nbox, const mfg_geom& g) {
         key.push_back(g.domain_lo[d]);
         key.push_back(g.domain_hi[d]);
     }
+    for (int d = 0; d < 3; ++d) key.push_back(g.is_periodic[d] ? 1 : 0);
     for (int b = 0; b < nbox; ++b)
         for (int d = 0; d < 3; ++d) {
             key.push_back(boxes[b].lo[d]);
@@ -186,6 +207,63 @@ cudaError_t ensure_owner(const mfg_box* boxes, int nbox, const mfg_geom& g) {
     }
     if ((e = cudaMemcpy(g_fill.d_owner, own.data(), own.size() * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
         return e;
+    // Slabs: per direction the grown extent splits into below / inside /
+    // above the domain (one range when periodic); every combination with at
+    // least one outside range is a slab of the stage = number of those.
+    std::vector<BcSlab> sl[3];
+    for (int b = 0; b < nbox; ++b) {
+        int rlo[3][3], rhi[3][3], rout[3][3], nr[3];
+        for (int d = 0; d < 3; ++d) {
+            const int glo = boxes[b].lo[d] - MFG_NGROW, ghi = boxes[b].hi[d] + MFG_NGROW;
+            const int dlo = g.domain_lo[d], dhi = g.domain_hi[d];
+            nr[d] = 0;
+            auto add = [&](int a, int z, int out) {
+                if (a > z) return;
+                rlo[d][nr[d]] = a;
+                rhi[d][nr[d]] = z;
+                rout[d][nr[d]] = out;
+                ++nr[d];
+            };
+            if (g.is_periodic[d]) {
+                add(glo, ghi, 0);
+            } else {
+                add(glo, std::min(ghi, dlo - 1), 1);
+                add(std::max(glo, dlo), std::min(ghi, dhi), 0);
+                add(std::max(glo, dhi + 1), ghi, 1);
+            }
+        }
+        for (int c = 0; c < nr[2]; ++c)
+            for (int bb = 0; bb < nr[1]; ++bb)
+                for (int a = 0; a < nr[0]; ++a) {
+                    const int r[3] = {a, bb, c};
+                    int nout = 0;
+                    BcSlab x;
+                    x.box = b;
+                    for (int d = 0; d < 3; ++d) {
+                        nout += rout[d][r[d]];
+                        x.lo[d] = rlo[d][r[d]];
+                        x.len[d] = rhi[d][r[d]] - rlo[d][r[d]] + 1;
+                    }
+                    if (nout) sl[nout - 1].push_back(x);
+                }
+    }
+    std::vector<BcSlab> all;
+    for (int q = 0; q < 3; ++q) {
+        g_fill.soff[q] = (int)all.size();
+        g_fill.nslab[q] = (int)sl[q].size();
+        g_fill.smax[q] = 0;
+        for (const BcSlab& x : sl[q]) g_fill.smax[q] = std::max<int64_t>(g_fill.smax[q], (int64_t)x.len[0] * x.len[1] * x.len[2]);
+        all.insert(all.end(), sl[q].begin(), sl[q].end());
+    }
+    if (all.size() > g_fill.scap) {
+        if (g_fill.d_slabs) cudaFree(g_fill.d_slabs);
+        g_fill.d_slabs = nullptr;
+        if ((e = cudaMalloc(&g_fill.d_slabs, all.size() * sizeof(BcSlab))) != cudaSuccess) return e;
+        g_fill.scap = all.size();
+    }
+    if (!all.empty() &&
+        (e = cudaMemcpy(g_fill.d_slabs, all.data(), all.size() * sizeof(BcSlab), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return e;
     g_fill.gran = gr;
     for (int d = 0; d < 3; ++d) g_fill.mlen[d] = ml[d];
     g_fill.key = key;
@@ -197,6 +275,7 @@ cudaError_t ensure_owner(const mfg_box* boxes, int nbox, const mfg_geom& g) {
 void fill_release() {
     if (g_fill.d_owner) cudaFree(g_fill.d_owner);
     if (g_fill.d_boxes) cudaFree(g_fill.d_boxes);
+    if (g_fill.d_slabs) cudaFree(g_fill.d_slabs);
     g_fill = OwnerCache();
 }
 
@@ -252,16 +331,19 @@ cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g,
         ProfScope ps(K_FILL_COPY, st);
         copy_kernel<<<grid, TPB, 0, st>>>(tab, G, g_fill.d_owner, nc);
     }
-    const bool any_phys = !(g.is_periodic[0] && g.is_periodic[1] && g.is_periodic[2]);
-    if (any_phys) {
-        const int ns = c_host_params().nspec;
-        for (int s = 1; s <= 3; ++s) {
+    const int ns = c_host_params().nspec;
+    for (int s = 1; s <= 3; ++s) {
+        // faces, then edges, then corners; at most 65535 slabs per launch
+        for (int s0 = 0; s0 < g_fill.nslab[s - 1]; s0 += 65535) {
+            const int cnt = std::min(65535, g_fill.nslab[s - 1] - s0);
+            const BcSlab* sl = g_fill.d_slabs + g_fill.soff[s - 1] + s0;
+            dim3 gb((unsigned)((g_fill.smax[s - 1] + TPB - 1) / TPB), (unsigned)cnt);
             ProfScope ps(K_FILL_BC, st);
-            if (ns <= 1) bc_kernel<1><<<grid, TPB, 0, st>>>(tab, G, s, nc);
-            else if (ns <= 2) bc_kernel<2><<<grid, TPB, 0, st>>>(tab, G, s, nc);
-            else if (ns <= 4) bc_kernel<4><<<grid, TPB, 0, st>>>(tab, G, s, nc);
-            else if (ns <= 8) bc_kernel<8><<<grid, TPB, 0, st>>>(tab, G, s, nc);
-            else bc_kernel<16><<<grid, TPB, 0, st>>>(tab, G, s, nc);
+            if (ns <= 1) bc_kernel<1><<<gb, TPB, 0, st>>>(tab, sl, G, s, nc);
+            else if (ns <= 2) bc_kernel<2><<<gb, TPB, 0, st>>>(tab, sl, G, s, nc);
+            else if (ns <= 4) bc_kernel<4><<<gb, TPB, 0, st>>>(tab, sl, G, s, nc);
+            else if (ns <= 8) bc_kernel<8><<<gb, TPB, 0, st>>>(tab, sl, G, s, nc);
+            else bc_kernel<16><<<gb, TPB, 0, st>>>(tab, sl, G, s, nc);
         }
     }
     return cudaGetLastError();
