@@ -204,8 +204,26 @@ cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Whether f holds exactly the valid box, components one after the other,
+// with no padding (then a copy of it is one contiguous block).
+static bool dense_over(const Fab& f, const mfg_box& b) {
+    const int64_t l0 = b.hi[0] - b.lo[0] + 1, l1 = b.hi[1] - b.lo[1] + 1, l2 = b.hi[2] - b.lo[2] + 1;
+    return f.p && f.b0 == b.lo[0] && f.b1 == b.lo[1] && f.b2 == b.lo[2] && f.js == l0 && f.ks == l0 * l1 &&
+           f.ns == l0 * l1 * l2;
+}
+
 cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, double a, bool copy_first,
                               const Fab& base, int ncomp, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+    if (copy_first && !src.p && !capturing && dense_over(dst, b) && dense_over(base, b)) {
+        // a plain copy of two dense arrays (phi_old <- phi_new): one block
+        // copy at the copy bandwidth instead of a kernel per (cell, component)
+        // (graphs keep the kernel: their conditional bodies take kernels)
+        ProfScope ps(K_COPY, st, 0);
+        if (dst.p == base.p) return cudaSuccess;
+        return cudaMemcpyAsync(dst.p, base.p, (size_t)ncomp * dst.ns * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    }
     Valid v = valid_of(b);
     dim3 g(nblocks(v.n), ncomp);
     ProfScope ps(K_COPY, st);
