@@ -314,6 +314,9 @@ int mfg_cutcells(const mfg_box* boxes, int nbox, const mfg_geom* geom, double ti
     if (rc) return rc;
     if (!geom) return MFG_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    const int lv = launch_cutcells_level(boxes, nbox, *geom, st);
+    if (lv < 0) return MFG_ERR_CUDA;
+    if (lv > 0) return MFG_OK;
     size_t need = 0;
     for (int b = 0; b < nbox; ++b) {
         size_t n = 1;

@@ -12,7 +12,9 @@
 //
 // Work layout: a compaction pass lists the box's cut cells (one atomic per
 // warp), then a fixed grid of threads walks the list, one cut cell per thread,
-// so no lane idles on pure fluid or solid cells.
+// so no lane idles on pure fluid or solid cells.  With the cache, a level's
+// boxes run in one launch per phase (launch_cutcells_level), box after box so
+// that each box's Sborder stays in L2 while its cut cells gather from it.
 //
 // Cut-cell cache: the list and the weights depend on the volume fraction of
 // the grown box only, while the reference recomputes them for every stage of
@@ -31,6 +33,7 @@
 // fraction changed are dropped by cutcache_sweep (called where the host
 // synchronizes anyway) and rebuilt by the next call.
 #include <algorithm>
+#include <cstring>
 #include <unordered_map>
 #include <vector>
 
@@ -138,6 +141,116 @@ __global__ void __launch_bounds__(TPB) cutcell_cached_kernel(CutBox c, CutCacheV
         cutcell_cached<NS>(c, (int)w, cc);
 }
 
+// ---- all boxes of a level in one launch per phase -------------------------
+// One box of the level table: its cut-cell geometry, stored entries, grown
+// volume-fraction copy and change flag.
+struct LevelCutBox {
+    CutBox c;
+    CutCacheView v;
+    unsigned ncut;
+    unsigned* dirty;
+    double* vf;
+    int glo[3], glen[3];  // grown box
+};
+
+// Clears every box's change flag and rebuilt-list count.
+__global__ void cut_level_reset_kernel(const LevelCutBox* __restrict__ tab, int nbox, unsigned* __restrict__ cnt) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nbox) {
+        *tab[b].dirty = 0;
+        cnt[b] = 0;
+    }
+}
+
+// Grown volume fraction against the stored copy (blockIdx.y = box).
+__global__ void cut_level_vf_kernel(const LevelCutBox* __restrict__ tab) {
+    const LevelCutBox& L = tab[blockIdx.y];
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)L.glen[0] * L.glen[1] * L.glen[2];
+    bool diff = false;
+    if (t < n) {
+        int i, j, k;
+        split3(t, L.glen[0], L.glen[1], i, j, k);
+        const double v = L.c.S(L.glo[0] + i, L.glo[1] + j, L.glo[2] + k, VFRAC);
+        diff = __double_as_longlong(v) != __double_as_longlong(L.vf[t]);
+    }
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) atomicOr(L.dirty, 1u);
+}
+
+// For a box whose volume fraction changed: its cut cells listed afresh
+// (grid-stride over the box; one atomic per warp).
+__global__ void cut_level_list_kernel(const LevelCutBox* __restrict__ tab, unsigned* __restrict__ cnt,
+                                      int* __restrict__ lists, int64_t cap) {
+    const LevelCutBox& L = tab[blockIdx.y];
+    if (!*L.dirty) return;
+    const CutBox& c = L.c;
+    int* list = lists + (int64_t)blockIdx.y * cap;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < c.n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = base + threadIdx.x;
+        bool cut = false;
+        if (t < c.n) {
+            int i, j, k;
+            cell_of(c, t, i, j, k);
+            const double vf = c.S(i, j, k, VFRAC);
+            cut = vf > 0.0 && vf < 1.0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cut);
+        if (!m) continue;
+        const int lane = threadIdx.x & 31;
+        unsigned at = 0;
+        if (lane == __ffs(m) - 1) at = atomicAdd(cnt + blockIdx.y, (unsigned)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, __ffs(m) - 1);
+        if (cut) list[at + __popc(m & ((1u << lane) - 1u))] = (int)t;
+    }
+}
+
+// Stored entries of every unchanged box: one warp per group of 32 list
+// positions, box after box (a box's Sborder stays in L2 while its groups
+// run), each box's groups in its own sorted order.
+template <int NS>
+__global__ void __launch_bounds__(TPB) cutcell_level_kernel(const LevelCutBox* __restrict__ tab,
+                                                            const int2* __restrict__ groups, unsigned ngroups) {
+    const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= ngroups) return;
+    const int2 bg = groups[gw];
+    const LevelCutBox& L = tab[bg.x];
+    if (*L.dirty) return;
+    const unsigned w = 32u * (unsigned)bg.y + (threadIdx.x & 31);
+    if (w < L.ncut) cutcell_cached<NS>(L.c, (int)w, L.v);
+}
+
+// Level tables (drivers alternate levels, so a few are kept), each rebuilt
+// when an entry is built or freed (g_cache_gen) or a box descriptor
+// changes; the rebuilt-list scratch is shared.
+struct CutLevelTable {
+    unsigned long long gen = ~0ull, used = 0;
+    std::vector<char> key;
+    LevelCutBox* d_tab = nullptr;
+    int2* d_groups = nullptr;
+    size_t tab_cap = 0, grp_cap = 0;
+    unsigned ngroups = 0;
+    int64_t cap = 0;  // list capacity per box (cells of the largest box)
+    int64_t maxgrown = 0;
+};
+constexpr int kLevelTables = 4;
+struct CutLevelCache {
+    CutLevelTable t[kLevelTables];
+    unsigned long long clock = 0;
+    unsigned* d_cnt = nullptr;
+    int* d_lists = nullptr;
+    size_t cnt_cap = 0, list_cap = 0;
+} g_level;
+
+void level_release() {
+    for (CutLevelTable& x : g_level.t) {
+        cudaFree(x.d_tab);
+        cudaFree(x.d_groups);
+    }
+    cudaFree(g_level.d_cnt);
+    cudaFree(g_level.d_lists);
+    g_level = CutLevelCache();
+}
+
 double g_wdir_dx[3] = {-1.0, -1.0, -1.0};
 
 struct CutEntry {
@@ -158,6 +271,10 @@ struct CutEntry {
     CutCacheView view() const { return {list, kc, base, off, wn, wd, scal}; }
 };
 
+// Bumped whenever an entry is built or freed: the level tables below are
+// keyed by it.
+unsigned long long g_cache_gen = 0;
+
 struct CutCache {
     std::unordered_map<const double*, CutEntry> map;
     unsigned* dirty = nullptr;  // one flag per slot
@@ -169,6 +286,7 @@ struct CutCache {
 } g_cache;
 
 void free_entry(CutEntry& e) {
+    ++g_cache_gen;
     cudaFree(e.vf);
     cudaFree(e.list);
     cudaFree(e.kc);
@@ -277,6 +395,7 @@ bool build_entry(const mfg_box& b, const CutBox& c, const mfg_geom& g, CutEntry&
         if (cudaStreamSynchronize(st) != cudaSuccess) return false;
     }
     g_cache.bytes += ng * sizeof(double) + 2 * c.n * sizeof(int) + need;
+    ++g_cache_gen;
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -316,6 +435,7 @@ void cutcache_sweep() {
 }
 
 void cutcache_release() {
+    level_release();
     for (auto& kv : g_cache.map) free_entry(kv.second);
     g_cache.map.clear();
     cudaFree(g_cache.dirty);
@@ -330,8 +450,9 @@ void cutcache_enable(bool on) {
     g_cache.enabled = on;
 }
 
-cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, int* list,
-                                unsigned* count, cudaStream_t st) {
+namespace {
+
+CutBox make_cutbox(const mfg_box& b, const mfg_geom& g, double* tcht_scratch) {
     CutBox c;
     c.n = 1;
     for (int d = 0; d < 3; ++d) {
@@ -343,25 +464,152 @@ cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tch
     c.S = make_fab(b.sborder);
     c.dxmin = fmin(g.dx[0], fmin(g.dx[1], g.dx[2]));
     c.tcht = tcht_scratch;
-    // the table depends on the cell aspect ratios only (dx / dxmin), the same on every level
-    const double dnk[3] = {g.dx[0] / c.dxmin, g.dx[1] / c.dxmin, g.dx[2] / c.dxmin};
-    if (dnk[0] != g_wdir_dx[0] || dnk[1] != g_wdir_dx[1] || dnk[2] != g_wdir_dx[2]) {
-        // Dirichlet weights: 1/((l dx_nd)^2 + (m dy_nd)^2 + (n dz_nd)^2 + 1e-40), centre unused
-        double w[SW * SW * SW];
-        const double dn[3] = {g.dx[0] / c.dxmin, g.dx[1] / c.dxmin, g.dx[2] / c.dxmin};
-        for (int n = -SG; n <= SG; ++n)
-            for (int m = -SG; m <= SG; ++m)
-                for (int l = -SG; l <= SG; ++l) {
-                    const double a = l * dn[0], bb = m * dn[1], e = n * dn[2];
-                    const double d2 = (a * a + bb * bb) + e * e;
-                    w[(l + SG) + SW * ((m + SG) + SW * (n + SG))] = (l == 0 && m == 0 && n == 0) ? 0.0 : 1.0 / (d2 + kTiny2);
-                }
-        cudaError_t e = cudaMemcpyToSymbolAsync(c_wdir, w, sizeof(w), 0, cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return e;
-        cudaStreamSynchronize(st);
-        for (int d = 0; d < 3; ++d) g_wdir_dx[d] = dnk[d];
-        cutcache_release();  // stored weights used the previous table
+    return c;
+}
+
+// The Dirichlet weight table depends on the cell aspect ratios only (dx /
+// dxmin), the same on every level; a new table drops the stored weights.
+cudaError_t ensure_wdir(const mfg_geom& g, double dxmin, cudaStream_t st) {
+    const double dnk[3] = {g.dx[0] / dxmin, g.dx[1] / dxmin, g.dx[2] / dxmin};
+    if (dnk[0] == g_wdir_dx[0] && dnk[1] == g_wdir_dx[1] && dnk[2] == g_wdir_dx[2]) return cudaSuccess;
+    // Dirichlet weights: 1/((l dx_nd)^2 + (m dy_nd)^2 + (n dz_nd)^2 + 1e-40), centre unused
+    double w[SW * SW * SW];
+    for (int n = -SG; n <= SG; ++n)
+        for (int m = -SG; m <= SG; ++m)
+            for (int l = -SG; l <= SG; ++l) {
+                const double a = l * dnk[0], bb = m * dnk[1], e = n * dnk[2];
+                const double d2 = (a * a + bb * bb) + e * e;
+                w[(l + SG) + SW * ((m + SG) + SW * (n + SG))] = (l == 0 && m == 0 && n == 0) ? 0.0 : 1.0 / (d2 + kTiny2);
+            }
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_wdir, w, sizeof(w), 0, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    cudaStreamSynchronize(st);
+    for (int d = 0; d < 3; ++d) g_wdir_dx[d] = dnk[d];
+    cutcache_release();  // stored weights used the previous table
+    return cudaSuccess;
+}
+
+template <class T>
+bool grow_buf(T*& p, size_t& have, size_t want) {
+    if (want <= have) return true;
+    cudaFree(p);
+    p = nullptr;
+    have = 0;
+    if (cudaMalloc(&p, want * sizeof(T)) != cudaSuccess) return false;
+    have = want;
+    return true;
+}
+
+// The table of this box layout, built (synchronizing) when missing; null when
+// it would have to be built during stream capture or memory is short.
+CutLevelTable* level_prepare(const std::vector<LevelCutBox>& tab) {
+    const size_t bytes = tab.size() * sizeof(LevelCutBox);
+    ++g_level.clock;
+    for (CutLevelTable& x : g_level.t)
+        if (x.gen == g_cache_gen && x.key.size() == bytes && std::memcmp(x.key.data(), tab.data(), bytes) == 0) {
+            x.used = g_level.clock;
+            return &x;
+        }
+    // the table and scratch about to be replaced may be read by kernels of an
+    // earlier call, on any stream
+    if (cudaDeviceSynchronize() != cudaSuccess) return nullptr;
+    CutLevelTable* T = &g_level.t[0];
+    for (CutLevelTable& x : g_level.t)
+        if (x.used < T->used) T = &x;
+    const int nbox = (int)tab.size();
+    std::vector<int2> groups;
+    int64_t cap = 1, maxgrown = 1;
+    for (int b = 0; b < nbox; ++b) {
+        const unsigned ng = (tab[b].ncut + 31) / 32;
+        for (unsigned q = 0; q < ng; ++q) groups.push_back(make_int2(b, (int)q));
+        cap = std::max<int64_t>(cap, tab[b].c.n);
+        maxgrown = std::max<int64_t>(maxgrown, (int64_t)tab[b].glen[0] * tab[b].glen[1] * tab[b].glen[2]);
     }
+    T->gen = ~0ull;  // invalid until filled
+    if (!grow_buf(T->d_tab, T->tab_cap, tab.size())) return nullptr;
+    if (!grow_buf(T->d_groups, T->grp_cap, std::max<size_t>(groups.size(), 1))) return nullptr;
+    if (!grow_buf(g_level.d_cnt, g_level.cnt_cap, tab.size())) return nullptr;
+    if (!grow_buf(g_level.d_lists, g_level.list_cap, (size_t)cap * nbox)) return nullptr;
+    if (cudaMemcpy(T->d_tab, tab.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    if (!groups.empty() &&
+        cudaMemcpy(T->d_groups, groups.data(), groups.size() * sizeof(int2), cudaMemcpyHostToDevice) != cudaSuccess)
+        return nullptr;
+    T->ngroups = (unsigned)groups.size();
+    T->cap = cap;
+    T->maxgrown = maxgrown;
+    T->key.assign(reinterpret_cast<const char*>(tab.data()), reinterpret_cast<const char*>(tab.data()) + bytes);
+    T->gen = g_cache_gen;
+    T->used = g_level.clock;
+    return T;
+}
+
+}  // namespace
+
+// All boxes of a level in four launches (change flags cleared, volume
+// fractions checked, lists of changed boxes rebuilt, stored entries applied)
+// plus one on-the-fly launch per box that does work only where the box's
+// volume fraction changed (the cache-off kernel itself, so those boxes give
+// that path's results by construction).  Returns 1 when done, -1 on a CUDA
+// error, and 0, having launched nothing, where the per-box path must run:
+// cache off, conjugate heat transfer (its neighbour-temperature scratch is
+// per box), a box without an entry, or a table to build during capture.
+int launch_cutcells_level(const mfg_box* boxes, int nbox, const mfg_geom& g, cudaStream_t st) {
+    if (nbox < 2 || !g_cache.enabled || c_host_params().conj_ht) return 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 0;
+    const double dxmin = fmin(g.dx[0], fmin(g.dx[1], g.dx[2]));
+    if (ensure_wdir(g, dxmin, st) != cudaSuccess) return -1;
+    std::vector<LevelCutBox> tab(nbox);
+    std::vector<int> slots(nbox);
+    for (int b = 0; b < nbox; ++b) {
+        LevelCutBox& L = tab[b];
+        memset(&L, 0, sizeof(L));
+        L.c = make_cutbox(boxes[b], g, nullptr);
+        CutEntry* ce = find_entry(boxes[b], L.c, g, st);
+        if (!ce) return 0;
+        slots[b] = ce->slot;
+        L.v = ce->view();
+        L.ncut = ce->ncut;
+        L.vf = ce->vf;
+        for (int d = 0; d < 3; ++d) {
+            L.glo[d] = boxes[b].lo[d] - 3;
+            L.glen[d] = L.c.len[d] + 6;
+        }
+    }
+    // find_entry may have grown the flag array: flag pointers last
+    for (int b = 0; b < nbox; ++b) tab[b].dirty = g_cache.dirty + slots[b];
+    CutLevelTable* T = level_prepare(tab);
+    if (!T) {
+        cudaGetLastError();  // an allocation refused here is not an error of the step
+        return 0;
+    }
+    const int ns = c_host_params().nspec;
+    ProfScope ps(K_CUT, st, 4 + nbox);
+    cut_level_reset_kernel<<<(nbox + 127) / 128, 128, 0, st>>>(T->d_tab, nbox, g_level.d_cnt);
+    cut_level_vf_kernel<<<dim3((unsigned)((T->maxgrown + 255) / 256), (unsigned)nbox), 256, 0, st>>>(T->d_tab);
+    cut_level_list_kernel<<<dim3(8, (unsigned)nbox), TPB, 0, st>>>(T->d_tab, g_level.d_cnt, g_level.d_lists, T->cap);
+    const unsigned nb = std::max(1u, (unsigned)(((uint64_t)T->ngroups * 32 + TPB - 1) / TPB));
+#define MFG_LEVEL_LAUNCH(K)                                                                                 \
+    do {                                                                                                    \
+        cutcell_level_kernel<K><<<nb, TPB, 0, st>>>(T->d_tab, T->d_groups, T->ngroups);                   \
+        for (int b = 0; b < nbox; ++b)                                                                      \
+            cutcell_kernel<K><<<152, TPB, 0, st>>>(tab[b].c, g_level.d_lists + (int64_t)b * T->cap,         \
+                                                   g_level.d_cnt + b);                                      \
+    } while (0)
+    if (ns <= 1) MFG_LEVEL_LAUNCH(1);
+    else if (ns <= 2) MFG_LEVEL_LAUNCH(2);
+    else if (ns <= 4) MFG_LEVEL_LAUNCH(4);
+    else if (ns <= 8) MFG_LEVEL_LAUNCH(8);
+    else MFG_LEVEL_LAUNCH(16);
+#undef MFG_LEVEL_LAUNCH
+    return cudaGetLastError() == cudaSuccess ? 1 : -1;
+}
+
+cudaError_t launch_cutcells_box(const mfg_box& b, const mfg_geom& g, double* tcht_scratch, int* list,
+                                unsigned* count, cudaStream_t st) {
+    CutBox c = make_cutbox(b, g, tcht_scratch);
+    cudaError_t we = ensure_wdir(g, c.dxmin, st);
+    if (we != cudaSuccess) return we;
     const unsigned nb = (unsigned)((c.n + TPB - 1) / TPB);
     const int ns = c_host_params().nspec;
     CutEntry* ce = find_entry(b, c, g, st);

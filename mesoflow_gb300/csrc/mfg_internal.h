@@ -109,6 +109,9 @@ cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g,
 // Cut-cell cache (mfg_ib.cu): drop entries whose volume fraction changed
 // (after a host synchronization), free everything, switch on/off.
 void cutcache_sweep();
+// All boxes of a level in one launch per phase: 1 done, 0 the per-box path
+// must run (nothing launched), -1 CUDA error (mfg_ib.cu).
+int launch_cutcells_level(const mfg_box* boxes, int nbox, const mfg_geom& g, cudaStream_t st);
 void cutcache_release();
 void cutcache_enable(bool on);
 
