@@ -124,7 +124,7 @@ def replica_value(cells, steps, world, ms):
     return cells * steps * world / (ms / 1e3)
 
 
-def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=4):
+def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=32):
     """The oracle (OpenMP build) on a bounded sample: the same workload
     generator at n=128 with 32^3 boxes; returns (cell-updates/s, threads, sample)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
