@@ -108,6 +108,55 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def step_traffic(a, cells):
+    """DRAM bytes of one step from the committed ncu launch list of the same
+    workload at a smaller size (profiles/step_traffic.json), scaled by the
+    cells processed (the per-box work is the same, so traffic grows with the
+    number of boxes)."""
+    p = os.path.join(ROOT, "profiles", "step_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f).get(f"{a.workload}_order{a.order}_grid{a.max_grid}")
+    if not d:
+        return None
+    return {"bytes_per_step": d["dram_bytes_per_step"] * cells / d["cells"],
+            "source": f"profiles/step_traffic.json: ncu dram__bytes_read.sum + dram__bytes_write.sum over the "
+                      f"{d['launches']} launches of one step at {d['n']}^3, scaled by cells"}
+
+
+def flop_count(a):
+    p = os.path.join(ROOT, "tests", "golden", "flops_per_cell_update.json")
+    if a.workload != "ib" or not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(f"porous_ib_{a.n}_order{a.order}")
+
+
+def extras(a):
+    """The batched AMR form and the adjoint form on their benchmark
+    configurations, each in a child process (each calls mfg_init with its own
+    tables), time-boxed; their JSON lines are summarised here."""
+    out = {}
+    runs = {"amr": ["--workload", "amr", "--steps", "2", "--warmup", "1"],
+            "adjoint": ["--workload", "adjoint", "--n", "128", "--adj-steps", "50", "--checkpoint", "10",
+                        "--steps", "1", "--warmup", "1"]}
+    for name, args in runs.items():
+        t0 = time.time()
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__)] + args, capture_output=True, text=True,
+                               timeout=900)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": f"rc {r.returncode}: " + (r.stderr or r.stdout)[-400:]}
+                continue
+            out[name] = json.loads(lines[-1])
+        except subprocess.TimeoutExpired:
+            out[name] = {"error": "timed out after 900 s"}
+        out[name]["wall_s"] = time.time() - t0
+    return out
+
+
 def max_over_ranks(ms, dist, device):
     """The slowest rank's time: every replica's timed region is bracketed by
     barriers, and the whole job's throughput uses the maximum."""
@@ -124,13 +173,34 @@ def replica_value(cells, steps, world, ms):
     return cells * steps * world / (ms / 1e3)
 
 
-def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=32):
-    """The oracle (OpenMP build) on a bounded sample: the same workload
-    generator at n=128 with 32^3 boxes; returns (cell-updates/s, threads, sample)."""
+def cpu_model():
+    """Host CPU model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def cpu_port_time(a, case=None, min_steps=3, min_seconds=10.0, max_steps=32):
+    """The oracle (OpenMP build, all host threads) on the same workload as the
+    GPU arm (same size and box layout): one untimed warm-up step, then at
+    least min_steps full RK3 steps (and at least min_seconds); returns
+    (cell-updates/s, threads, sample)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_run import OracleLevel
-    ns = 128
-    case = make_case(a, n=ns, max_grid=32)
+    if case is None:
+        case = make_case(a)
     o = OracleLevel(case, variant="omp")
     dt = o.est_timestep()
     o.advance(dt)  # warm-up
@@ -140,12 +210,12 @@ def cpu_port_time(a, steps=None, min_seconds=10.0, max_steps=32):
         o.advance(dt)
         k += 1
         el = time.perf_counter() - t0
-        if (steps is not None and k >= steps) or (steps is None and (el >= min_seconds or k >= max_steps)):
+        if k >= max_steps or (k >= min_steps and el >= min_seconds):
             break
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     cells = case.n_cell[0] * case.n_cell[1] * case.n_cell[2]
-    sample = (f"{ns}^3 instance of the same generator ({len(case.boxes)} boxes of 32^3), {k} RK3 steps after 1 "
-              f"warm-up, {el:.1f} s wall, OpenMP over boxes")
+    sample = (f"the same workload ({case.n_cell[0]}^3, {len(case.boxes)} boxes of {a.max_grid}^3), {k} full RK3 "
+              f"steps after 1 warm-up, {el:.1f} s wall, OpenMP over boxes, {threads} threads on {cpu_model()}")
     return cells * k / el, threads, sample
 
 
@@ -153,14 +223,16 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    v, th, sample = cpu_port_time(a, steps=None)
+    v, th, sample = cpu_port_time(a)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "higher_is_better": True,
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(a)}, "scaling": "weak", "vs_baseline": None,
+            "config": {"workload": workload_name(a), "cells": a.n ** 3, "order_hyp": a.order}, "scaling": "weak",
+            "vs_baseline": None,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference cannot be built here (its AMReX submodule is not vendored, no MPI); "
-                    "this arm times the oracle, a line-by-line CPU restatement of its numerics"}
+            "note": "the reference application cannot be built here (its AMReX submodule is not vendored, no MPI); "
+                    "this arm times the oracle, a CPU restatement of its numerics that equals the reference's own "
+                    "per-cell code bit for bit (tests/test_cpu_ref_pin.py)"}
     print(json.dumps(line))
     return 0
 
@@ -188,9 +260,9 @@ def algorithmic(kind, case, a, nlaunch_per_step):
 
 def run_amr(a):
     """Batched AMR form vs plain per-box launches of the same kernels on the
-    3-level catalyst hierarchy (base 128^3, ratio 2, ~1400 uneven boxes of
-    16-64 cells, properly nested, 8 gas + 2 site species, 8 Arrhenius surface
-    reactions, WENO5).  Headline: the reference's multi-level coarse step
+    3-level catalyst hierarchy (base 128^3 in 64^3 boxes, ratio 2, finer
+    levels in uneven boxes of 16-32 cells per side: 1488 boxes, properly
+    nested, 8 gas + 2 site species, 8 Arrhenius surface reactions, WENO5).  Headline: the reference's multi-level coarse step
     (levels subcycled, two-level fill with conservative interpolation, flux
     registers, reflux, average-down); also the common-dt form of the same
     hierarchy.  A cell-update is one cell advanced one step of its level."""
@@ -199,7 +271,7 @@ def run_amr(a):
     from mesoflow_gb300.level import MultiLevel
     torch.cuda.set_device(0)
     lib = abi.load()
-    amr = cases.catalyst_amr(n0=128, nlev=3, order=5)
+    amr = cases.catalyst_amr(n0=128, nlev=3, order=5, base_grid=64, max_grid=32)
     abi.check("mfg_init", lib.mfg_init(C.byref(amr.params)))
     ml = MultiLevel(amr, backend="torch", device="cuda:0")
     h = C.c_void_p()
@@ -280,78 +352,104 @@ def run_amr(a):
 
 
 def run_adjoint(a):
-    """Adjoint form: wall time of one gradient evaluation (J, dJ/dlog A_r for 8
-    reactions and dJ/du_in through the hand-written adjoint of the whole step)
-    against the same nsteps plain steps plus the objective, on the catalyst
-    case (8 gas + 2 site species, WENO5, velocity inlet) at n^3 in 32^3 boxes.
-    Both with every step's intermediates kept in HBM (checkpoint_every 0) and
-    with checkpoints every 5 steps (recomputation)."""
+    """Adjoint form on the adjoint benchmark configuration: wall time of one
+    gradient evaluation (J, dJ/dlog A_r for 8 reactions and dJ/du_in through
+    the hand-written adjoint of the whole step) against the same nsteps plain
+    steps plus the objective, on the catalyst case (catalyst block + seeded
+    sphere pack, solid fraction 0.3, seed 5; 8 gas + 2 site species, WENO5,
+    velocity inlet) at n^3 in 32^3 boxes, with checkpoints every
+    a.checkpoint steps (bounded memory); also with every step's
+    intermediates kept when they fit in device memory.  Peak device memory in
+    use is sampled during each run."""
+    import threading
+
     import torch
     from mesoflow_gb300 import abi, cases
     from mesoflow_gb300.adjoint import ReactionProblem
-    from mesoflow_gb300.driver import Mflo
     torch.cuda.set_device(0)
     lib = abi.load()
     n = a.n if a.n != 256 else 128
-    case = cases.catalyst(n=n, order=5, max_grid=32)
+    case = cases.catalyst(n=n, order=5, max_grid=32, seed=5)
     nsteps = a.adj_steps
-    dt = Mflo(case, device="cuda:0").est_timestep()
+    p = ReactionProblem(case, nsteps, 0.0)
     logA = [math.log(case.params.A[r]) for r in range(case.params.nreact)]
     u_in = case.meta["u_in"]
+    p.reset(logA, u_in)
+    dt_c = C.c_double()
+    st0 = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    abi.check("mfg_est_timestep", lib.mfg_est_timestep(p.desc, len(case.boxes), C.byref(case.geom), 0.0,
+                                                       C.byref(dt_c), st0))
+    dt = dt_c.value
     nb = len(case.boxes)
     g = C.byref(case.geom)
+    total_mem = torch.cuda.mem_get_info()[1]
 
-    def timed(p, fn):
+    def timed(fn):
         p.reset(logA, u_in)
         torch.cuda.synchronize()
+        used = [0]
+        stop = threading.Event()
+
+        def sample():
+            while not stop.is_set():
+                free, tot = torch.cuda.mem_get_info()
+                used[0] = max(used[0], tot - free)
+                time.sleep(0.02)
+
+        th = threading.Thread(target=sample, daemon=True)
+        th.start()
         s = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
-        fn(p, C.c_void_p(s.cuda_stream))
+        J = fn(C.c_void_p(s.cuda_stream))
         e1.record(s)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
+        stop.set()
+        th.join()
+        return e0.elapsed_time(e1), used[0], J
 
-    def forward(p, st):
+    def forward(st):
         for i in range(nsteps):
             abi.check("mfg_advance_level", lib.mfg_advance_level(p.desc, nb, g, i * dt, dt, 0, 1, None, st))
         J = C.c_double()
         abi.check("mfg_reaction_objective", lib.mfg_reaction_objective(p.desc, nb, g, C.byref(J), st))
+        return J.value
 
     def adjoint(ce):
-        def fn(p, st):
+        def fn(st):
             J, gu = C.c_double(), C.c_double()
             gA = (C.c_double * 16)()
             abi.check("mfg_adjoint_objective", lib.mfg_adjoint_objective(p.desc, nb, g, nsteps, dt, ce, C.byref(J),
                                                                          gA, C.byref(gu), st))
+            return J.value
         return fn
 
-    p = ReactionProblem(case, nsteps, dt)
-    reps = max(1, a.steps // 2)
-    res = {}
-    for name, fn in (("forward", forward), ("adjoint_keep_all", adjoint(0)), ("adjoint_checkpoint5", adjoint(5))):
-        for _ in range(1):
-            timed(p, fn)
-        ms = sorted(timed(p, fn) for _ in range(reps))
-        res[name] = ms[len(ms) // 2]
-    lib.mfg_profile(1)
-    timed(p, adjoint(0))
-    kk = 32
-    kms, kcnt = (C.c_double * kk)(), (C.c_longlong * kk)()
-    nk = lib.mfg_profile_read(kms, kcnt, kk)
-    lib.mfg_profile(0)
-    kernels = {lib.mfg_profile_name(i).decode(): {"ms": kms[i], "launches": kcnt[i]} for i in range(nk) if kcnt[i]}
     cells = n ** 3
+    runs = [("forward", forward), (f"adjoint_checkpoint{a.checkpoint}", adjoint(a.checkpoint))]
+    keep_bytes = nsteps * cells * 8 * 345 * 1.1  # snapshots of every step: about 345 doubles per cell and step
+    if keep_bytes < 0.8 * total_mem:
+        runs.append(("adjoint_keep_all", adjoint(0)))
+    res, mem, Js = {}, {}, {}
+    for name, fn in runs:
+        for _ in range(a.warmup):
+            timed(fn)
+        ms = sorted(timed(fn) for _ in range(max(1, a.steps)))
+        res[name], mem[name], Js[name] = ms[len(ms) // 2]
+    ck = f"adjoint_checkpoint{a.checkpoint}"
     out = {"metric": "adjoint / forward wall-time ratio (gradient of the surface reaction rate)",
-           "value": res["adjoint_keep_all"] / res["forward"], "unit": "x", "higher_is_better": False,
-           "n_gpus": 1, "steps": reps, "warmup": 1, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"catalyst {n}^3 in {nb} boxes of 32^3, 8 gas + 2 site species, 8 Arrhenius "
-                                  f"surface reactions, WENO5, velocity inlet, {nsteps} steps of dt {dt:.3e}",
+           "value": res[ck] / res["forward"], "unit": "x", "higher_is_better": False,
+           "n_gpus": 1, "steps": max(1, a.steps), "warmup": a.warmup, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"catalyst {n}^3 in {nb} boxes of 32^3 (block + seeded spheres, solid 0.3, "
+                                  f"seed 5), 8 gas + 2 site species, 8 Arrhenius surface reactions, WENO5, velocity "
+                                  f"inlet, {nsteps} steps of dt {dt:.3e}, checkpoint every {a.checkpoint}",
                       "gradient": "J and dJ/dlog A_r (8) and dJ/du_in"},
-           "ms": res,
-           "ratio_checkpoint5": res["adjoint_checkpoint5"] / res["forward"],
-           "gradient_cell_steps_per_s": cells * nsteps / (res["adjoint_keep_all"] / 1e3),
-           "kernels_keep_all": kernels}
+           "ms": res, "peak_device_bytes_in_use": mem,
+           "J": Js["forward"],
+           "J_max_rel_diff_across_modes": max(abs(v - Js["forward"]) for v in Js.values()) / abs(Js["forward"]),
+           "ratio_keep_all": res["adjoint_keep_all"] / res["forward"] if "adjoint_keep_all" in res else None,
+           "keep_all_skipped": None if "adjoint_keep_all" in res else
+           f"every step's intermediates need about {keep_bytes / 1e9:.0f} GB",
+           "gradient_cell_steps_per_s": cells * nsteps / (res[ck] / 1e3)}
     print(json.dumps(out))
     return 0
 
@@ -366,13 +464,18 @@ def main():
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--max-grid", dest="max_grid", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-extras", dest="no_extras", action="store_true",
+                    help="skip the batched-AMR and adjoint runs appended to the default line")
+    ap.add_argument("--checkpoint", type=int, default=10,
+                    help="adjoint workload: checkpoint_every of the bounded-memory run")
     ap.add_argument("--workload", default="ib", choices=["ib", "tg", "amr", "adjoint"],
                     help="ib: the 256^3 immersed-boundary workload (default); tg: 256^3 5-species Taylor-Green "
                          "(use --order 5); amr: batched vs plain on 3 levels; adjoint: gradient vs forward time "
                          "on the catalyst case (--n, default 128)")
     ap.add_argument("--adj-steps", dest="adj_steps", type=int, default=10)
     a = ap.parse_args()
-    a.warmup = max(a.warmup, 3)
+    if a.workload in ("ib", "tg"):
+        a.warmup = max(a.warmup, 3)
     if a.impl == "reference":
         return run_reference(a)
     if a.workload == "amr":
@@ -422,11 +525,13 @@ def main():
     clocks = Clocks(local)
     l0 = lib.mfg_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("mfg_timed_steps")  # lets ncu select the timed launches (--nvtx-include)
     e0.record(stream)
     for _ in range(a.steps):
         step(t)
         t += dt
     e1.record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     launches = lib.mfg_launch_count() - l0
     ms = e0.elapsed_time(e1)
@@ -475,53 +580,72 @@ def main():
     lib.mfg_profile(0)
     kernels = {lib.mfg_profile_name(i).decode(): {"ms": kms[i], "launches": kcnt[i]} for i in range(nk) if kcnt[i]}
     tot = sum(v["ms"] for v in kernels.values())
+    peaks, src = read_peaks()
+    hbm = peaks.get("hbm_gbs")
+    step_ms = ms / a.steps
+    per_replica = value / world
+
+    # HBM roofline of the step: 64 N algorithmic bytes per cell-update (stage 1
+    # reads U^n and writes U^1, stages 2-3 read the stage input and U^n and write
+    # the output), over the CUDA-event time of the step.
+    abytes_cell = 64 * case.ncomp
+    achieved = per_replica * abytes_cell / 1e9
+    traffic = step_traffic(a, cells)
+    roof = {"bound": "hbm", "kernel": "rk3 step (one mfg_advance_level: fill, cut cells, 3 x face + update, "
+                                      "chemistry sub-step, primitive refresh, clipping, residual norms)",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": traffic["bytes_per_step"] if traffic else None, "peak_source": src,
+            "algorithmic_bytes_per_cell_update": abytes_cell, "algorithmic_bytes_per_step": abytes_cell * cells,
+            "step_ms": step_ms, "traffic_source": traffic["source"] if traffic else None}
+
+    # the dominant kernel on its own: its byte model per launch over its launch time
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     avg_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
-    peaks, src = read_peaks()
     # the face pass of orders 1/2 covers the three directions of a box in one
     # timed entry (split + list kernels); the per-direction figures scale by 3
     dirs = 3 if (dom == "face" and a.order <= 2) else 1
-    abytes = dirs * algorithmic(dom, case, a, kernels[dom]["launches"])
-    achieved = abytes / (avg_ms / 1e3) / 1e9
-    # per-launch DRAM traffic and FP64 flop of the dominant kernel from the committed ncu capture
-    counts = {}
-    cpath = os.path.join(ROOT, "profiles", "kernel_counts.json")
-    if os.path.exists(cpath):
-        with open(cpath) as f:
-            counts = json.load(f).get(dom, {})
-    traffic = counts.get("dram_bytes_per_launch") if counts.get("order_hyp") == a.order else None
-    traffic = dirs * traffic if traffic else traffic
+    kbytes = dirs * algorithmic(dom, case, a, kernels[dom]["launches"])
+    kach = kbytes / (avg_ms / 1e3) / 1e9
+    kroof = {"kernel": dom, "achieved": kach, "peak": hbm, "unit": "GB/s", "frac": kach / hbm,
+             "model_bytes_per_launch": kbytes, "avg_launch_ms": avg_ms, "directions_per_launch": dirs,
+             "share_of_step": kernels[dom]["ms"] / tot if tot else None,
+             "note": "bytes of a per-kernel traffic model (inputs and outputs of the kernel, intermediates included), "
+                     "not the step's algorithmic bytes"}
+
+    # FP64: the binding roof.  Algorithmic FP64 operations per cell-update of
+    # the reference's own per-cell code (counting build), over the live DFMA peak.
     fp64_peak = C.c_double()
     abi.check("mfg_measure_fp64_peak", lib.mfg_measure_fp64_peak(C.byref(fp64_peak), st))
-    flop = counts.get("fp64_flop_per_launch") if counts.get("order_hyp") == a.order else None
-    flop = dirs * flop if flop else flop
     fp64 = None
-    if flop:
-        ach = flop / (avg_ms / 1e3) / 1e12
+    fc = flop_count(a)
+    if fc:
+        ach = per_replica * fc["flop_per_cell_update"] / 1e12
         fp64 = {"achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s", "frac": ach / fp64_peak.value,
-                "flop_per_launch": flop, "flop_source": "profiles/kernel_counts.json (ncu)",
+                "flop_per_cell_update": fc["flop_per_cell_update"],
+                "divisions_per_cell_update": fc["divisions_per_cell_update"],
+                "flop_source": "tests/golden/flops_per_cell_update.json: FP64 operations of the reference's own "
+                               "per-cell code (counting build), " + fc["sample"],
                 "peak_source": "measured live: mfg_measure_fp64_peak (DFMA loop, FMA = 2 flop)"}
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-            "frac": achieved / peaks.get("hbm_gbs"), "traffic": traffic, "peak_source": src,
-            "algorithmic_bytes_per_launch": abytes, "avg_launch_ms": avg_ms, "directions_per_launch": dirs,
-            "share_of_step": kernels[dom]["ms"] / tot if tot else None, "fp64": fp64,
-            "binding_roof": "fp64 issue (the stencil needs ~10^3 FP64 ops per cell per RHS against ~64 N bytes per cell-update)"}
 
-    out = {"metric": METRIC_TG if a.workload == "tg" else METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
-           "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic",
+    out = {"metric": METRIC_TG if a.workload == "tg" else METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": workload_name(a), "cells": cells, "boxes": nb, "order_hyp": a.order,
                       "dt": dt, "l2": "inputs larger than L2 (state %.2f GB)" % (h2d / 1e9),
                       "parallelism": f"replicas x{world}"},
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d},
-           "gpu_launches": launches, "clocks": clk, "roofline": roof,
+           "gpu_launches": launches, "clocks": clk, "roofline": roof, "kernel_roofline": kroof, "fp64": fp64,
+           "binding_roof": "fp64 issue (the stencil needs ~10^3 FP64 operations per cell per RHS against "
+                           "64 N bytes per cell-update)",
            "kernels_ms_per_step": {k: v["ms"] for k, v in kernels.items()},
-           "fp64_peak_tflops_live": fp64_peak.value,
-           "algorithmic_bytes_per_cell_update": 64 * case.ncomp,
-           "step_hbm_roofline_frac": value / world * 64 * case.ncomp / (peaks.get("hbm_gbs") * 1e9)}
-    if rank == 0 and not a.no_cpu:
-        v, th, sample = cpu_port_time(a)
+           "fp64_peak_tflops_live": fp64_peak.value}
+    if rank == 0 and world == 1 and not a.no_cpu:
+        v, th, sample = cpu_port_time(a, case)
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": th, "kind": "port", "sample": sample}
+    if rank == 0 and world == 1 and not a.no_extras and a.workload == "ib":
+        del lev, host
+        torch.cuda.empty_cache()
+        out["extras"] = extras(a)
     if rank == 0:
         print(json.dumps(out))
     if dist:

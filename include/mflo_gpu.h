@@ -211,7 +211,8 @@ typedef struct mfg_params {
  * chemistry.H, species.cpp) and mflo::ReadParameters (Source/mflo.cpp:263-307). */
 int mfg_init(const mfg_params* params);
 
-/* Frees the library's scratch (face fluxes, box tables, graphs). */
+/* Frees the library's scratch (face fluxes, box tables, graphs) and forgets
+ * the device addresses cached by mfg_compute_dsdt_flow_noalloc. */
 int mfg_finalize(void);
 
 /* Reads (and optionally clears) the sticky device status bits.  Synchronizes. */
@@ -232,7 +233,9 @@ int mfg_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom* geom,
 
 /* Immersed-boundary cut-cell ghost treatment, in place on sborder (valid cells).
  * Replaces mflo::update_cutcell_data (Source/mflo_evolve.cpp:495-519)
- * -> update_cutcells (Source/Src_3d/ib_utils.H:272-436). */
+ * -> update_cutcells (Source/Src_3d/ib_utils.H:272-436).  The level-wide form
+ * of the pass keeps its cut-cell lists in one library buffer: calls must be
+ * ordered on one stream (or synchronized); calls that overlap on the GPU race. */
 int mfg_cutcells(const mfg_box* boxes, int nbox, const mfg_geom* geom,
                  double time, void* stream);
 
@@ -358,7 +361,8 @@ int mfg_update_vars_after_chemsolve(const mfg_box* boxes, int nbox, int using_bg
  * A box whose scratch exceeds the array returns MFG_ERR_SIZE (any 32^3 box
  * fits, for every species count; a 40^3 box does not).  All calls share the array: calls that overlap on
  * the GPU race.  The first call on each device looks up the array's device
- * address; make it before any stream capture.  No counterpart in the
+ * address; make it before any stream capture (after a cudaDeviceReset, call
+ * mfg_finalize first so that the address is looked up again).  No counterpart in the
  * reference, which allocates its flux and transport FABs per box
  * (Source/mflo_evolve.cpp:566-591). */
 int mfg_compute_dsdt_flow_noalloc(const mfg_box* boxes, int nbox, const mfg_geom* geom,
@@ -465,9 +469,14 @@ int mfg_reaction_objective(const mfg_box* boxes, int nbox, const mfg_geom* geom,
  * normal velocity of the velocity-inlet boundaries, the initial state held
  * fixed).  Both gradient pointers may be null.  checkpoint_every > 0: the
  * state is kept every checkpoint_every steps and the steps between are
- * recomputed during the reverse sweep (device memory: about
+ * recomputed during the reverse sweep.  When one segment's intermediates fit
+ * in free device memory (about checkpoint_every x (6 level-sized and 6 grown
+ * arrays) plus nsteps/checkpoint_every level-sized ones), each segment but
+ * the last is recomputed once with its intermediates kept and then reversed
+ * (the last segment keeps them from the first forward sweep); otherwise each
+ * step is recomputed once more before its reverse (about
  * nsteps/checkpoint_every + checkpoint_every + 10 level-sized arrays and 5
- * grown ones); checkpoint_every = 0: every step's intermediates are kept and
+ * grown ones).  checkpoint_every = 0: every step's intermediates are kept and
  * nothing is recomputed (about 3 level-sized and 3 grown arrays per step).
  * The gradients do not depend on the choice beyond rounding.  Supported: order_hyp 5,
  * do_ns 1, molar or mass-single thermo, constant viscosity and conductivity,

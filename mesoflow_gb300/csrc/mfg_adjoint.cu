@@ -1729,12 +1729,26 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
     const bool keep_all = checkpoint_every == 0;
     const int ce = keep_all ? 1 : std::min(checkpoint_every, nsteps);
     const int nseg = keep_all ? 0 : (nsteps + ce - 1) / ce;
-    std::vector<double*> ckpt(nseg), zst(keep_all ? 0 : ce);
+    // With checkpoints, the snapshots of one whole segment are kept when they
+    // fit in device memory: each segment is then recomputed once (the last one
+    // not at all: its snapshots come from the first forward sweep) and reversed
+    // from its snapshots.  Otherwise one snapshot is kept: the segment's states
+    // are recomputed and stored, and each step is recomputed once more with its
+    // snapshot before its reverse.
+    const size_t snap_doubles = 3 * (W.gtot * (size_t)W.N + W.gtot * (size_t)NAUX + W.fstot) + 3 * W.vtot * (size_t)W.N;
+    bool seg_keep = false;
+    if (!keep_all) {
+        size_t free_b = 0, total_b = 0;
+        ADJ_TRY(cudaMemGetInfo(&free_b, &total_b), "memory query");
+        const size_t need = (size_t)ce * snap_doubles * sizeof(double) + ((size_t)nseg + 6) * W.vtot * W.N * sizeof(double);
+        seg_keep = need + (size_t)2 * 1024 * 1024 * 1024 < free_b;
+    }
+    std::vector<double*> ckpt(nseg), zst((keep_all || seg_keep) ? 0 : ce);
     for (auto& p : ckpt)
         if (!(p = W.valid_buf())) return MFG_ERR_CUDA;
     for (auto& p : zst)
         if (!(p = W.valid_buf())) return MFG_ERR_CUDA;
-    std::vector<Snap> snaps(keep_all ? nsteps : 1);
+    std::vector<Snap> snaps(keep_all ? nsteps : seg_keep ? ce : 1);
     for (Snap& sn : snaps) {
         for (int s = 0; s < 3; ++s)
             if (!(sn.sb[s] = W.grown_buf(W.N)) || !(sn.aux[s] = W.grown_buf(NAUX)) ||
@@ -1777,10 +1791,13 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
                     "restore");
         return MFG_OK;
     };
-    // forward sweep with checkpoints (or with every step's intermediates)
+    // forward sweep with checkpoints (or with every step's intermediates); with
+    // whole-segment snapshots the last segment keeps them here already
+    const int last0 = keep_all ? 0 : (nseg - 1) * ce;
     for (int n = 0; n < nsteps; ++n) {
         if (!keep_all && n % ce == 0 && (rc = save(ckpt[n / ce]))) return rc;
-        if ((rc = fwd_step(W, dt, keep_all ? &snaps[n] : nullptr, st))) return rc;
+        const Snap* keep = keep_all ? &snaps[n] : (seg_keep && n >= last0) ? &snaps[n - last0] : nullptr;
+        if ((rc = fwd_step(W, dt, keep, st))) return rc;
     }
     // objective and its seed on the final state
     ADJ_TRY(cudaMemsetAsync(lam, 0, W.vtot * W.N * sizeof(double), st), "clear");
@@ -1793,6 +1810,16 @@ extern "C" int mfg_adjoint_objective(const mfg_box* boxes, int nbox, const mfg_g
     // reverse sweep, one checkpoint segment at a time
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int n0 = seg * ce, n1 = std::min(nsteps, n0 + ce);
+        if (seg_keep) {
+            if (seg != nseg - 1) {
+                if ((rc = restore(ckpt[seg]))) return rc;
+                for (int n = n0; n < n1; ++n)
+                    if ((rc = fwd_step(W, dt, &snaps[n - n0], st))) return rc;
+            }
+            for (int n = n1 - 1; n >= n0; --n)
+                if ((rc = adj_step(W, dt, snaps[n - n0], lam, lamOld, lamL, lamSb, lamAux, st))) return rc;
+            continue;
+        }
         if ((rc = restore(ckpt[seg]))) return rc;
         for (int n = n0; n < n1; ++n) {
             if ((rc = save(zst[n - n0]))) return rc;

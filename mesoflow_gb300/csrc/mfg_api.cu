@@ -282,6 +282,7 @@ int mfg_finalize(void) {
     g_pool = Pool();
     fill_release();
     cutcache_release();
+    noalloc_forget();
     g_ready = false;
     return MFG_OK;
 }
@@ -491,19 +492,27 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, doub
         if ((rc = mfg_cutcells(boxes, nbox, geom, time, stream))) return rc;
         if ((rc = run_rhs(boxes, nbox, geom, stage, dt, st))) return rc;
     }
-    if (!only_flow) {
-        for (int b = 0; b < nbox; ++b)
-            if (launch_axpy_valid(boxes[b], make_fab(boxes[b].s_old), none, 0.0, true, make_fab(boxes[b].s_new), N,
-                                  st) != cudaSuccess)
-                return MFG_ERR_CUDA;
-        if ((rc = mfg_chem_substep(boxes, nbox, geom, time, dt, stream))) return rc;
+    // the bookends in one pass per box: phi_old <- phi_new and the chemistry
+    // sub-step (unless only_flow), primitive refresh, clipping, residual norms
+    double *part = nullptr, *acc = nullptr;
+    const size_t npart = (size_t)N * 1024;
+    if (resnorms) {
+        if (pool_reserve((npart + N) * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
+        part = reinterpret_cast<double*>(g_pool.p);
+        acc = part + npart;
+        if (cudaMemsetAsync(acc, 0, N * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
     }
-    if ((rc = mfg_update_primitive_vars(boxes, nbox, geom, stream))) return rc;
-    if (clip && (rc = mfg_clip_species(boxes, nbox, stream))) return rc;
-    if (resnorms && (rc = mfg_residual_norms(boxes, nbox, dt, resnorms, stream))) return rc;
+    for (int b = 0; b < nbox; ++b)
+        if (launch_post_step(boxes[b], dt, !only_flow, clip != 0, part, acc, st) != cudaSuccess) return MFG_ERR_CUDA;
+    std::vector<double> hn(resnorms ? N : 0);
+    if (resnorms && cudaMemcpyAsync(hn.data(), acc, N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return MFG_ERR_CUDA;
     unsigned v = 0;
     if (cudaStreamSynchronize(st) != cudaSuccess || read_status(&v, false) != cudaSuccess) return MFG_ERR_CUDA;
     cutcache_sweep();
+    if (resnorms)
+        for (int n = 0; n < N; ++n) resnorms[n] = std::sqrt(hn[n]);
+    if (v & MFG_STATUS_NEG_PRESSURE) return MFG_ERR_NEG_PRESSURE;
     if (v & MFG_STATUS_NAN) return MFG_ERR_NAN;
     return MFG_OK;
 }

@@ -29,7 +29,9 @@ enum KernelKind {
     K_PRIM = 0, K_FACE, K_FLUX, K_UPDATE, K_FILL_COPY, K_FILL_BC, K_CUT, K_CHEM, K_PRIMS, K_CLIP,
     K_RESNORM, K_TIMESTEP, K_COPY,
     // adjoint (mfg_adjoint.cu)
-    K_ADJ_FACE, K_ADJ_CELL, K_ADJ_CUT, K_ADJ_FILL, K_ADJ_LOCAL, K_SNAPSHOT, K_ADJ_FLUX, K_AMR_SYNC, K_AMR_PATCH, K_AMR_INTERP, K_COUNT
+    K_ADJ_FACE, K_ADJ_CELL, K_ADJ_CUT, K_ADJ_FILL, K_ADJ_LOCAL, K_SNAPSHOT, K_ADJ_FLUX, K_AMR_SYNC, K_AMR_PATCH, K_AMR_INTERP,
+    // fused step bookends (mfg_step.cu)
+    K_POST, K_COUNT
 };
 
 // Counts one launch; when profiling is on, brackets it with CUDA events on its stream.
@@ -101,6 +103,8 @@ cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, 
 cudaError_t launch_update_prims(const mfg_box& b, double* minp_slot, cudaStream_t st);
 cudaError_t launch_split_chem(const mfg_box& b, int kind, double dt, int bg, cudaStream_t st);
 cudaError_t launch_clip_species(const mfg_box& b, cudaStream_t st);
+cudaError_t launch_post_step(const mfg_box& b, double dt, bool chem, bool clip, double* partial, double* acc,
+                             cudaStream_t st);
 cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st);
 
 cudaError_t launch_fill_patch(const mfg_box* boxes, int nbox, const mfg_geom& g, int s_src, double time,
@@ -114,5 +118,8 @@ void cutcache_sweep();
 int launch_cutcells_level(const mfg_box* boxes, int nbox, const mfg_geom& g, cudaStream_t st);
 void cutcache_release();
 void cutcache_enable(bool on);
+// Allocation-free entry point (mfg_noalloc.cu): forget the per-device addresses
+// of its static scratch array.
+void noalloc_forget();
 
 }  // namespace mfg

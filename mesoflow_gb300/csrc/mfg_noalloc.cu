@@ -22,8 +22,13 @@
 //    (different streams, or different host threads without ordering) race on
 //    the array; serialize them.
 //  * The device address of the array is looked up once per device, on the
-//    first call made with that device current.  Make that first call before
-//    any stream capture begins.
+//    first call made with that device current (host threads may make that
+//    first call concurrently).  Make that first call before any stream
+//    capture begins.  mfg_finalize forgets the addresses: after a
+//    cudaDeviceReset, call mfg_finalize before this entry point runs again.
+#include <atomic>
+#include <mutex>
+
 #include "mfg_internal.h"
 
 namespace mfg {
@@ -32,23 +37,38 @@ namespace {
 static __device__ __align__(256) double g_noalloc_scratch[MFG_NOALLOC_SCRATCH_DOUBLES];
 
 constexpr int kMaxDevices = 64;
-double* g_scratch_ptr[kMaxDevices] = {nullptr};
+std::atomic<double*> g_scratch_ptr[kMaxDevices];
+std::mutex g_scratch_mu;
 
 // Device address of the static array for the current device (host code may not
 // use the symbol itself: on the host it names a stand-in, not device memory).
 int scratch_for_current_device(double** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return MFG_ERR_CUDA;
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return MFG_ERR_CUDA;
-        g_scratch_ptr[dev] = static_cast<double*>(p);
+    double* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        p = g_scratch_ptr[dev].load(std::memory_order_relaxed);
+        if (!p) {
+            void* q = nullptr;
+            if (cudaGetSymbolAddress(&q, g_noalloc_scratch) != cudaSuccess || !q) return MFG_ERR_CUDA;
+            p = static_cast<double*>(q);
+            g_scratch_ptr[dev].store(p, std::memory_order_release);
+        }
     }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return MFG_OK;
 }
 
 }  // namespace
+
+// Forgets the looked-up addresses (mfg_finalize), so that the next call looks
+// them up again in the current context.
+void noalloc_forget() {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    for (auto& p : g_scratch_ptr) p.store(nullptr, std::memory_order_release);
+}
+
 }  // namespace mfg
 
 using namespace mfg;

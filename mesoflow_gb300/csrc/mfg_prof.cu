@@ -10,7 +10,7 @@ namespace {
 const char* kNames[K_COUNT] = {"prim", "face", "flux", "update", "fill_copy", "fill_bc",
                                "cutcell", "chem", "prims", "clip", "resnorm", "timestep", "copy",
                                "adj_face", "adj_cell", "adj_cut", "adj_fill", "adj_local", "snapshot",
-                               "adj_flux", "amr_sync", "amr_patch", "amr_interp"};
+                               "adj_flux", "amr_sync", "amr_patch", "amr_interp", "post"};
 
 struct Pending {
     int kind;

@@ -62,6 +62,51 @@ __global__ void resnorm_kernel(Valid v, Fab Sn, Fab So, double a, double b, doub
     }
 }
 
+// The bookends of a box after the RK3 stages in one pass (post_cell: phi_old
+// <- phi_new and the chemistry sub-step when chem, primitive refresh, species
+// clipping when clip) and, when partial != nullptr, the block partial sums of
+// the residual norms ((s_new - s_old)/dt, flow components scaled by the old
+// volume fraction; warp-shuffle reduction, partials in block order).
+template <int NS>
+__global__ void __launch_bounds__(TPB, 2) post_step_kernel(Valid v, Fab So, Fab Sn, double dt, int chem, int clip,
+                                                        double a, double b, double* partial, int nblk) {
+    constexpr int NM = NFLO + NS;
+    const int N = NFLO + c_P.nspec;
+    double acc[NM];
+#pragma unroll
+    for (int n = 0; n < NM; ++n) acc[n] = 0.0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += (int64_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(v, t, i, j, k);
+        double u[NM], o[NM];
+        post_cell<NS>(So, Sn, i, j, k, dt, chem != 0, clip != 0, partial != nullptr, u, o);
+        if (partial) {
+#pragma unroll
+            for (int n = 0; n < NM; ++n) {
+                if (n >= N) continue;
+                // LinComb then Multiply, rounded as the reference (no contraction)
+                double d = add(mul(a, u[n]), mul(b, o[n]));
+                if (n < VFRAC) d = mul(d, o[VFRAC]);
+                acc[n] += d * d;
+            }
+        }
+    }
+    if (!partial) return;
+    __shared__ double ws[TPB / 32][NM];
+#pragma unroll
+    for (int n = 0; n < NM; ++n) {
+        double x = acc[n];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5][n] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double x = 0.0;
+        for (int w = 0; w < TPB / 32; ++w) x += ws[w][threadIdx.x];
+        partial[(int64_t)threadIdx.x * nblk + blockIdx.x] = x;
+    }
+}
+
 // Fixed-order final sum of the block partials, accumulated into acc[n].
 __global__ void resnorm_final_kernel(const double* partial, int nblk, double* acc) {
     const int n = blockIdx.x;
@@ -191,6 +236,28 @@ cudaError_t launch_resnorm_box(const mfg_box& b, double dt, double* partial, dou
     return cudaGetLastError();
 }
 
+// partial: scratch of (ncomp * 1024) doubles, acc: ncomp doubles (device), or
+// both null (no residual norms).
+cudaError_t launch_post_step(const mfg_box& b, double dt, bool chem, bool clip, double* partial, double* acc,
+                             cudaStream_t st) {
+    Valid v = valid_of(b);
+    const int ns = c_host_params().nspec, nc = NFLO + ns;
+    // 4 cells per thread: enough blocks to fill the GPU from one box
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + 4 * TPB - 1) / (4 * TPB)));
+    const double a = 1.0 / dt, bb = -1.0 / dt;
+    ProfScope ps(K_POST, st, partial ? 2 : 1);
+#define MFG_POST(NSB) post_step_kernel<NSB><<<nblk, TPB, 0, st>>>(v, make_fab(b.s_old), make_fab(b.s_new), dt, chem, \
+                                                                  clip, a, bb, partial, nblk)
+    if (ns <= 1) MFG_POST(1);
+    else if (ns <= 2) MFG_POST(2);
+    else if (ns <= 4) MFG_POST(4);
+    else if (ns <= 8) MFG_POST(8);
+    else MFG_POST(16);
+#undef MFG_POST
+    if (partial) resnorm_final_kernel<<<nc, 32, 0, st>>>(partial, nblk, acc);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_timestep(const mfg_box& b, double* acc2, cudaStream_t st) {
     Valid v = valid_of(b);
     Fab S = make_fab(b.s_new);
@@ -215,14 +282,25 @@ static bool dense_over(const Fab& f, const mfg_box& b) {
 cudaError_t launch_axpy_valid(const mfg_box& b, const Fab& dst, const Fab& src, double a, bool copy_first,
                               const Fab& base, int ncomp, cudaStream_t st) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    const bool capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing(st, &cs);
+    if (ce != cudaSuccess) return ce;
+    const bool capturing = cs != cudaStreamCaptureStatusNone;
     if (copy_first && !src.p && !capturing && dense_over(dst, b) && dense_over(base, b)) {
         // a plain copy of two dense arrays (phi_old <- phi_new): one block
         // copy at the copy bandwidth instead of a kernel per (cell, component)
-        // (graphs keep the kernel: their conditional bodies take kernels)
-        ProfScope ps(K_COPY, st, 0);
-        if (dst.p == base.p) return cudaSuccess;
-        return cudaMemcpyAsync(dst.p, base.p, (size_t)ncomp * dst.ns * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        // (graphs keep the kernel: their conditional bodies take kernels);
+        // arrays that overlap without being the same one take the kernel, whose
+        // per-cell copy is defined for them
+        const size_t bytes = (size_t)ncomp * dst.ns * sizeof(double);
+        if (dst.p == base.p) {
+            ProfScope ps(K_COPY, st, 0);
+            return cudaSuccess;
+        }
+        const char *d0 = reinterpret_cast<const char*>(dst.p), *b0 = reinterpret_cast<const char*>(base.p);
+        if (d0 + bytes <= b0 || b0 + bytes <= d0) {
+            ProfScope ps(K_COPY, st, 0);
+            return cudaMemcpyAsync(dst.p, base.p, bytes, cudaMemcpyDeviceToDevice, st);
+        }
     }
     Valid v = valid_of(b);
     dim3 g(nblocks(v.n), ncomp);

@@ -251,29 +251,20 @@ __device__ bool chem_ros2_cell(double* y, double temp, double dt) {
 // states S_i = S_old + sum_j (dt*a_ij) F_j, result S_old + sum_i (dt*w_i) F_i
 // (AMReX RKIntegrator with the SSPRK3 tableau: a21=1, a31=a32=1/4,
 // w=1/6,1/6,2/3).  Components without a source keep S_old.
+// Species of one cell after the explicit SSP-RK3 chemistry sub-step over dt
+// from s0 (the reference's AMReX TimeIntegrator, rk.type 3: nodes 0, 1, 1/2;
+// a21 = 1, a31 = a32 = 1/4; weights 1/6, 1/6, 2/3), or after the implicit
+// ROS2 sub-step; the flow components are not changed by it.
 template <int NS>
-__device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So, const Fab& Sn, double dt, int ncomp,
-                                                  int64_t t) {
-    if (t >= v.n) return;
-    int i, j, k;
-    cell_of(v, t, i, j, k);
+__device__ __forceinline__ void chem_species(const double* s0, double temp, double dt, double* out) {
     const int ns = c_P.nspec;
     if (c_P.chem_kind == 1) {  // implicit (ROS2) chemistry
-        double y[NS];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) y[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
-        chem_ros2_cell<NS>(y, So(i, j, k, TEMP), dt);
-        for (int n = 0; n < ncomp; ++n) {
-            if (n >= NFLO) continue;
-            Sn(i, j, k, n) = So(i, j, k, n);
-        }
-        for (int s = 0; s < ns; ++s) Sn(i, j, k, NFLO + s) = y[s];
+        for (int s = 0; s < NS; ++s) out[s] = s0[s];
+        chem_ros2_cell<NS>(out, temp, dt);
         return;
     }
-    double s0[NS], s1[NS], f0[NS], f1[NS], f2[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) s0[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
-    const double temp = So(i, j, k, TEMP);
+    double s1[NS], f0[NS], f1[NS], f2[NS];
     double kr[MAXR];
     rate_constants(temp, kr);
     spec_source_k<NS>(s0, kr, f0);
@@ -286,10 +277,6 @@ __device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So,
         s1[s] = add(add(s0[s], mul(c20, add(0.0, add(0.0, f0[s])))), mul(c21, add(0.0, add(0.0, f1[s]))));
     spec_source_k<NS>(s1, kr, f2);
     const double w0 = dt * (1.0 / 6.0), w1 = dt * (1.0 / 6.0), w2 = dt * (2.0 / 3.0);
-    for (int n = 0; n < ncomp; ++n) {
-        if (n >= NFLO) continue;
-        Sn(i, j, k, n) = So(i, j, k, n);
-    }
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         if (s >= ns) continue;
@@ -297,8 +284,28 @@ __device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So,
         r = add(r, mul(w0, add(0.0, add(0.0, f0[s]))));
         r = add(r, mul(w1, add(0.0, add(0.0, f1[s]))));
         r = add(r, mul(w2, add(0.0, add(0.0, f2[s]))));
-        Sn(i, j, k, NFLO + s) = r;
+        out[s] = r;
     }
+}
+
+template <int NS>
+__device__ __forceinline__ void chem_substep_body(const Valid& v, const Fab& So, const Fab& Sn, double dt, int ncomp,
+                                                  int64_t t) {
+    if (t >= v.n) return;
+    int i, j, k;
+    cell_of(v, t, i, j, k);
+    const int ns = c_P.nspec;
+    double s0[NS], s1[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) s0[s] = (s < ns) ? So(i, j, k, NFLO + s) : 0.0;
+    chem_species<NS>(s0, So(i, j, k, TEMP), dt, s1);
+    for (int n = 0; n < ncomp; ++n) {
+        if (n >= NFLO) continue;
+        Sn(i, j, k, n) = So(i, j, k, n);
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+        if (s < ns) Sn(i, j, k, NFLO + s) = s1[s];
 }
 
 // mflo::Advance_chemistry (Source/mflo_splitchem.cpp:177-199), the explicit
@@ -393,31 +400,50 @@ __device__ __forceinline__ void vars_after_chem_body(const Valid& v, const Fab& 
 
 // cons -> prim refresh (Source/mflo_evolve.cpp:114-171); negative pressure
 // raises a status bit instead of aborting.
+// update_primitive_vars of one cell held in registers (u: the NFLO flow
+// components, spec: the species), Source/mflo_evolve.cpp:114-171: in gas cells
+// the primitives from the conserved variables, in solid cells of a conjugate
+// heat transfer run the solid temperature; a negative pressure raises the
+// sticky status.  Returns a bit mask of the flow components it wrote.
+template <int NS>
+__device__ __forceinline__ unsigned prims_cell(double* u, const double* spec) {
+    const DevParams& P = c_P;
+    const double vf = u[VFRAC];
+    unsigned wrote = 0;
+    if (vf == 1.0) {
+        const double rho = u[RHO];
+        const double vx = u[RHOU] / rho, vy = u[RHOV] / rho, vz = u[RHOW] / rho;
+        const double rhoe = u[RHOE] - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
+        const double p = thermo_p<NS>(rhoe, rho, spec);
+        u[DENS] = rho;
+        u[VELX] = vx;
+        u[VELY] = vy;
+        u[VELZ] = vz;
+        u[PRES] = p;
+        u[TEMP] = thermo_t<NS>(rho, p, spec);
+        wrote = (1u << DENS) | (1u << VELX) | (1u << VELY) | (1u << VELZ) | (1u << PRES) | (1u << TEMP);
+    } else if (P.conj_ht && vf == 0.0) {
+        u[TEMP] = P.solid_temp;
+        wrote = 1u << TEMP;
+    }
+    if (P.do_ns && u[PRES] < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
+    return wrote;
+}
+
 template <int NS>
 __device__ __forceinline__ void prims_body(const Valid& v, const Fab& S, int64_t t) {
     if (t >= v.n) return;
     int i, j, k;
     cell_of(v, t, i, j, k);
-    const DevParams& P = c_P;
-    const double vf = S(i, j, k, VFRAC);
-    if (vf == 1.0) {
-        const double rho = S(i, j, k, RHO);
-        double spec[NS];
+    double u[NFLO], spec[NS];
 #pragma unroll
-        for (int s = 0; s < NS; ++s) spec[s] = (s < P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
-        const double vx = S(i, j, k, RHOU) / rho, vy = S(i, j, k, RHOV) / rho, vz = S(i, j, k, RHOW) / rho;
-        const double rhoe = S(i, j, k, RHOE) - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
-        const double p = thermo_p<NS>(rhoe, rho, spec);
-        S(i, j, k, DENS) = rho;
-        S(i, j, k, VELX) = vx;
-        S(i, j, k, VELY) = vy;
-        S(i, j, k, VELZ) = vz;
-        S(i, j, k, PRES) = p;
-        S(i, j, k, TEMP) = thermo_t<NS>(rho, p, spec);
-    } else if (P.conj_ht && vf == 0.0) {
-        S(i, j, k, TEMP) = P.solid_temp;
-    }
-    if (P.do_ns && S(i, j, k, PRES) < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
+    for (int n = 0; n < NFLO; ++n) u[n] = S(i, j, k, n);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) spec[s] = (s < c_P.nspec) ? S(i, j, k, NFLO + s) : 0.0;
+    const unsigned wrote = prims_cell<NS>(u, spec);
+#pragma unroll
+    for (int n = DENS; n <= TEMP; ++n)
+        if ((wrote >> n) & 1u) S(i, j, k, n) = u[n];
 }
 
 __device__ __forceinline__ void atomic_max_nonneg(double* a, double v) {
@@ -457,6 +483,60 @@ __device__ __forceinline__ void clip_body(const Valid& v, const Fab& S, int nspe
     cell_of(v, t, i, j, k);
     for (int s = 0; s < nspec; ++s)
         if (S(i, j, k, NFLO + s) < 0.0) S(i, j, k, NFLO + s) = 0.0;
+}
+
+// The step's bookends of one cell after the three RK3 stages, fused
+// (Source/mflo_evolve.cpp:33-58, 470-493, 521-540, 91-112): with chem,
+// phi_old <- phi_new and the chemistry sub-step phi_new = chem(phi_old); the
+// primitive refresh; species clipping when clip.  On return u holds the new
+// state of the cell (every component) and o the state phi_old holds, the
+// operands of the residual norms.  Reads the cell's components once and
+// writes only what changes.
+template <int NS>
+__device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, int j, int k, double dt, bool chem,
+                                          bool clip, bool need_old, double* u, double* o) {
+    const int ns = c_P.nspec;
+    double spec[NS];
+#pragma unroll
+    for (int n = 0; n < NFLO; ++n) u[n] = Sn(i, j, k, n);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? Sn(i, j, k, NFLO + s) : 0.0;
+    if (chem) {
+#pragma unroll
+        for (int n = 0; n < NFLO; ++n) {
+            So(i, j, k, n) = u[n];
+            o[n] = u[n];
+        }
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < ns) {
+                So(i, j, k, NFLO + s) = spec[s];
+                o[NFLO + s] = spec[s];
+            }
+        double s1[NS];
+        chem_species<NS>(spec, u[TEMP], dt, s1);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? s1[s] : 0.0;
+    } else if (need_old) {
+#pragma unroll
+        for (int n = 0; n < NFLO; ++n) o[n] = So(i, j, k, n);
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < ns) o[NFLO + s] = So(i, j, k, NFLO + s);
+    }
+    const unsigned wrote = prims_cell<NS>(u, spec);
+#pragma unroll
+    for (int n = DENS; n <= TEMP; ++n)
+        if ((wrote >> n) & 1u) Sn(i, j, k, n) = u[n];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        if (s >= ns) continue;
+        const double c0 = spec[s];
+        if (clip && spec[s] < 0.0) spec[s] = 0.0;
+        // stored when the sub-step or the clipping may have changed it
+        if (chem || spec[s] != c0 || (clip && c0 < 0.0)) Sn(i, j, k, NFLO + s) = spec[s];
+        u[NFLO + s] = spec[s];
+    }
 }
 
 }  // namespace

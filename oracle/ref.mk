@@ -32,14 +32,21 @@ CASES := \
 name_of = $(word 1,$(subst :, ,$(1)))
 dir_of  = $(word 2,$(subst :, ,$(1)))
 LIBS    := $(foreach c,$(CASES),$(OUT)/libref_$(call name_of,$(c)).so)
+# counting builds (Real = a double that counts FP64 operations, ref_shim/count_double.H)
+COUNTED := porous tg catcyl
+CLIBS   := $(foreach c,$(filter $(addsuffix :%,$(COUNTED)),$(CASES)),$(OUT)/libref_count_$(call name_of,$(c)).so)
 
-all: $(LIBS)
+all: $(LIBS) $(CLIBS)
 
 define case_rule
 $(OUT)/libref_$(call name_of,$(1)).so: ref_driver.cpp $(wildcard ref_shim/*.H) ../include/mflo_gpu.h
 	@mkdir -p $(OUT)
 	$(CXX) $(FLAGS) -Iref_shim -I$(REF)/$(call dir_of,$(1)) -I$(REF)/Source -I$(REF)/Source/Src_3d -I../include \
 	    -o $$@ ref_driver.cpp $(REF)/$(call dir_of,$(1))/species.cpp $(REF)/$(call dir_of,$(1))/userfuncs.cpp
+$(OUT)/libref_count_$(call name_of,$(1)).so: ref_driver.cpp $(wildcard ref_shim/*.H) ../include/mflo_gpu.h
+	@mkdir -p $(OUT)
+	$(CXX) $(FLAGS) -DMFG_COUNT_FLOPS -Iref_shim -I$(REF)/$(call dir_of,$(1)) -I$(REF)/Source -I$(REF)/Source/Src_3d \
+	    -I../include -o $$@ ref_driver.cpp $(REF)/$(call dir_of,$(1))/species.cpp $(REF)/$(call dir_of,$(1))/userfuncs.cpp
 endef
 $(foreach c,$(CASES),$(eval $(call case_rule,$(c))))
 

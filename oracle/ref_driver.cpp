@@ -19,6 +19,8 @@
 //                      ParallelFor order).
 //   ref_chem_source    mflo::compute_dsdt_chemistry (:684-720) on s_new:
 //                      dsdt = 0 + compute_spec_source.
+// Built with MFG_COUNT_FLOPS (libref_count_<case>.so), Real is a counting
+// double and ref_flop_counts reports the FP64 operations of those loops.
 // Nothing here is linked into the product library.
 #include <cstring>
 #include <vector>
@@ -40,7 +42,7 @@ namespace {
 
 amrex::Array4<amrex::Real> view(const mfg_array4& a) {
     amrex::Array4<amrex::Real> v;
-    v.p = a.p;
+    v.p = reinterpret_cast<amrex::Real*>(a.p);
     v.jstride = a.jstride;
     v.kstride = a.kstride;
     v.nstride = a.nstride;
@@ -89,8 +91,8 @@ int ref_init(void) {
     return 0;
 }
 
-double ref_molwt(int sp) { return mflo_species::molwts[sp]; }
-double ref_advect_flag(int sp) { return mflo_species::advect_flags[sp]; }
+double ref_molwt(int sp) { return static_cast<double>(mflo_species::molwts[sp]); }
+double ref_advect_flag(int sp) { return static_cast<double>(mflo_species::advect_flags[sp]); }
 
 int ref_compute_dsdt(const mfg_geom* G, const mfg_box* boxes, int nbox, double time, int order, double dissfactor,
                      int nsflag, int spec_in_solid, int conj_ht) {
@@ -189,5 +191,19 @@ int ref_chem_source(const mfg_geom* G, const mfg_box* boxes, int nbox, double ti
     }
     return MFG_OK;
 }
+
+#ifdef MFG_COUNT_FLOPS
+// FP64 operations counted since the last reset (count_double.H): add, mul,
+// div, sqrt, other.
+void ref_flop_counts(uint64_t* out, int reset) {
+    auto& c = mfg_count::counts();
+    out[0] = c.add;
+    out[1] = c.mul;
+    out[2] = c.div;
+    out[3] = c.sqrt;
+    out[4] = c.other;
+    if (reset) c = mfg_count::Counts();
+}
+#endif
 
 }  // extern "C"

@@ -17,6 +17,8 @@
 //   Abort          throws amrex_shim_abort (the driver turns it into a status)
 //   Print          discards its output
 //   ParmParse      queries leave their arguments unchanged (no inputs file)
+// With MFG_COUNT_FLOPS defined, Real is a counting double (count_double.H):
+// the same sources then report how many FP64 operations they perform.
 #ifndef MFG_AMREX_SHIM_H_
 #define MFG_AMREX_SHIM_H_
 
@@ -43,9 +45,17 @@
 #define AMREX_PRAGMA_SIMD
 #define AMREX_D_DECL(a, b, c) a, b, c
 
+#ifdef MFG_COUNT_FLOPS
+#include "count_double.H"
+#endif
+
 namespace amrex {
 
+#ifdef MFG_COUNT_FLOPS
+using Real = mfg_count::CD;
+#else
 using Real = double;
+#endif
 
 template <class T>
 using Vector = std::vector<T>;

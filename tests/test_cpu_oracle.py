@@ -13,7 +13,8 @@ import riemann
 from oracle_run import OracleLevel
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SOD = "/root/reference/tests/Cartesian/ShockTube_N2/exact_soln"
+REF_SOD = os.path.join(os.environ.get("MFLO_REFERENCE", "/root/reference"), "tests", "Cartesian", "ShockTube_N2",
+                       "exact_soln")
 
 
 def test_abi_layout_matches_c():

@@ -23,7 +23,7 @@ thermo families (molar with the mass- or molar-cv energy, single gas,
 background gas) in every plugin of the reference that defines one.
 
 The tests that build the libraries need the reference checkout
-(MFLO_REFERENCE, default /root/reference) and are skipped without it; the
+(the MFLO_REFERENCE variable, else ref_lib's default) and are skipped without it; the
 golden-fixture test needs only the oracle.
 """
 import ctypes as C
