@@ -846,52 +846,63 @@ __device__ __forceinline__ void flux5_sweep_body(const RhsBox& B, int d, int c, 
         }
         return;
     }
-    // raw values of cells f-3 .. f+2
+    // raw values of cells f-3 .. f+2; the per-cell WENO parts of the four
+    // stencil centres f-2 .. f+1 are built only when a face needs them: faces
+    // on the solid side of the immersed boundary (no hyperbolic flux) and
+    // first-order fallback faces use the raw values alone, so columns through
+    // solid regions skip the reconstruction's per-cell work (bitwise the same
+    // numbers: each centre is the same weno_cell of the same three values)
     double ru[6], rf[6];
 #pragma unroll
     for (int q = 0; q < 6; ++q) sweep_raw(B, d, c, sc, oR + (q - 3) * sd, xR + (q - 3) * xd, ru[q], rf[q]);
     WenoWindow w;
-    w.u0 = weno_cell(ru[0], ru[1], ru[2]);
-    w.u1 = weno_cell(ru[1], ru[2], ru[3]);
-    w.u2 = weno_cell(ru[2], ru[3], ru[4]);
-    w.u3 = weno_cell(ru[3], ru[4], ru[5]);
-    w.f0 = weno_cell(rf[0], rf[1], rf[2]);
-    w.f1 = weno_cell(rf[1], rf[2], rf[3]);
-    w.f2 = weno_cell(rf[2], rf[3], rf[4]);
-    w.f3 = weno_cell(rf[3], rf[4], rf[5]);
-    double uL = ru[2], uR = ru[3], uP1 = ru[4], uP2 = ru[5];
-    double fL = rf[2], fR = rf[3], fP1 = rf[4], fP2 = rf[5];
+    unsigned have = 0;  // bit q: centre f-2+q built
     for (int f = f0;; ++f) {
-        const double F = flux5_face(B, d, c, FS, qf, w, uL, uR, fL, fR, vfp[oR - sd], vfp[oR]);
+        const int flags = (int)__double_as_longlong(FS.p[qf + FS_FLAGS * FS.ns]);
+        if ((flags & 3) == 1) {
+            if (!(have & 1u)) {
+                w.u0 = weno_cell(ru[0], ru[1], ru[2]);
+                w.f0 = weno_cell(rf[0], rf[1], rf[2]);
+            }
+            if (!(have & 2u)) {
+                w.u1 = weno_cell(ru[1], ru[2], ru[3]);
+                w.f1 = weno_cell(rf[1], rf[2], rf[3]);
+            }
+            if (!(have & 4u)) {
+                w.u2 = weno_cell(ru[2], ru[3], ru[4]);
+                w.f2 = weno_cell(rf[2], rf[3], rf[4]);
+            }
+            if (!(have & 8u)) {
+                w.u3 = weno_cell(ru[3], ru[4], ru[5]);
+                w.f3 = weno_cell(rf[3], rf[4], rf[5]);
+            }
+            have = 15u;
+        }
+        const double F = flux5_face(B, d, c, FS, qf, w, ru[2], ru[3], rf[2], rf[3], vfp[oR - sd], vfp[oR]);
         Idx3 fi;
         fi.i = iv[0];
         fi.j = iv[1];
         fi.k = iv[2];
         flux5_store(B, d, c, sc, fi, F);
         if (f == f1) break;
-        // advance one face: load cell f+3, build the cell centred on f+2
+        // advance one face: load cell f+3, shift the window
         ++iv[d];
         oR += sd;
         xR += xd;
         qf += fd;
-        double un, fn;
-        sweep_raw(B, d, c, sc, oR + 2 * sd, xR + 2 * xd, un, fn);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            ru[q] = ru[q + 1];
+            rf[q] = rf[q + 1];
+        }
+        sweep_raw(B, d, c, sc, oR + 2 * sd, xR + 2 * xd, ru[5], rf[5]);
         w.u0 = w.u1;
         w.u1 = w.u2;
         w.u2 = w.u3;
-        w.u3 = weno_cell(uP1, uP2, un);
         w.f0 = w.f1;
         w.f1 = w.f2;
         w.f2 = w.f3;
-        w.f3 = weno_cell(fP1, fP2, fn);
-        uL = uR;
-        uR = uP1;
-        uP1 = uP2;
-        uP2 = un;
-        fL = fR;
-        fR = fP1;
-        fP1 = fP2;
-        fP2 = fn;
+        have = (have >> 1) & 7u;
     }
 }
 

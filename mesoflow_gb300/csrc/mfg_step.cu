@@ -66,44 +66,33 @@ __global__ void resnorm_kernel(Valid v, Fab Sn, Fab So, double a, double b, doub
 // <- phi_new and the chemistry sub-step when chem, primitive refresh, species
 // clipping when clip) and, when partial != nullptr, the block partial sums of
 // the residual norms ((s_new - s_old)/dt, flow components scaled by the old
-// volume fraction; warp-shuffle reduction, partials in block order).
-template <int NS>
-__global__ void __launch_bounds__(TPB, 2) post_step_kernel(Valid v, Fab So, Fab Sn, double dt, int chem, int clip,
-                                                        double a, double b, double* partial, int nblk) {
-    constexpr int NM = NFLO + NS;
+// volume fraction).  Each thread adds its cells' terms to its own slot of a
+// shared-memory table ([component][thread]); one warp per component then sums
+// the slots in a fixed order, so the partials are deterministic.
+constexpr int PTPB = 128;
+
+template <int NS, int CHEM>
+__global__ void __launch_bounds__(PTPB) post_step_kernel(Valid v, Fab So, Fab Sn, double dt, int clip, double a,
+                                                         double b, double* partial, int nblk) {
+    extern __shared__ double sacc[];  // [ncomp][PTPB] when partial
     const int N = NFLO + c_P.nspec;
-    double acc[NM];
-#pragma unroll
-    for (int n = 0; n < NM; ++n) acc[n] = 0.0;
+    double* mine = partial ? sacc + threadIdx.x : nullptr;
+    if (partial)
+        for (int n = 0; n < N; ++n) mine[n * PTPB] = 0.0;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of(v, t, i, j, k);
-        double u[NM], o[NM];
-        post_cell<NS>(So, Sn, i, j, k, dt, chem != 0, clip != 0, partial != nullptr, u, o);
-        if (partial) {
-#pragma unroll
-            for (int n = 0; n < NM; ++n) {
-                if (n >= N) continue;
-                // LinComb then Multiply, rounded as the reference (no contraction)
-                double d = add(mul(a, u[n]), mul(b, o[n]));
-                if (n < VFRAC) d = mul(d, o[VFRAC]);
-                acc[n] += d * d;
-            }
-        }
+        post_cell<NS, CHEM>(So, Sn, i, j, k, dt, clip != 0, a, b, mine, PTPB);
     }
     if (!partial) return;
-    __shared__ double ws[TPB / 32][NM];
-#pragma unroll
-    for (int n = 0; n < NM; ++n) {
-        double x = acc[n];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5][n] = x;
-    }
     __syncthreads();
-    if (threadIdx.x < N) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int n = warp; n < N; n += PTPB / 32) {
         double x = 0.0;
-        for (int w = 0; w < TPB / 32; ++w) x += ws[w][threadIdx.x];
-        partial[(int64_t)threadIdx.x * nblk + blockIdx.x] = x;
+#pragma unroll
+        for (int q = 0; q < PTPB / 32; ++q) x += sacc[n * PTPB + q * 32 + lane];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) partial[(int64_t)n * nblk + blockIdx.x] = x;
     }
 }
 
@@ -242,18 +231,27 @@ cudaError_t launch_post_step(const mfg_box& b, double dt, bool chem, bool clip, 
                              cudaStream_t st) {
     Valid v = valid_of(b);
     const int ns = c_host_params().nspec, nc = NFLO + ns;
-    // 4 cells per thread: enough blocks to fill the GPU from one box
-    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + 4 * TPB - 1) / (4 * TPB)));
+    // one cell per thread up to 1024 blocks, then a grid-stride loop
+    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + PTPB - 1) / PTPB));
     const double a = 1.0 / dt, bb = -1.0 / dt;
+    const size_t smem = partial ? (size_t)nc * PTPB * sizeof(double) : 0;
+    const DevParams& P = c_host_params();
+    // the sub-step of a zero source (no reactions, explicit integrator) is s + 0
+    const int kind = !chem ? 0 : (P.chem_kind == 0 && (!P.chem_on || P.nreact == 0)) ? 1 : 2;
     ProfScope ps(K_POST, st, partial ? 2 : 1);
-#define MFG_POST(NSB) post_step_kernel<NSB><<<nblk, TPB, 0, st>>>(v, make_fab(b.s_old), make_fab(b.s_new), dt, chem, \
-                                                                  clip, a, bb, partial, nblk)
-    if (ns <= 1) MFG_POST(1);
-    else if (ns <= 2) MFG_POST(2);
-    else if (ns <= 4) MFG_POST(4);
-    else if (ns <= 8) MFG_POST(8);
-    else MFG_POST(16);
+#define MFG_POST_K(NSB, K) post_step_kernel<NSB, K><<<nblk, PTPB, smem, st>>>(v, make_fab(b.s_old), \
+                                                   make_fab(b.s_new), dt, clip, a, bb, partial, nblk)
+#define MFG_POST(NSB)                     \
+    if (kind == 0) MFG_POST_K(NSB, 0);    \
+    else if (kind == 1) MFG_POST_K(NSB, 1); \
+    else MFG_POST_K(NSB, 2);
+    if (ns <= 1) { MFG_POST(1) }
+    else if (ns <= 2) { MFG_POST(2) }
+    else if (ns <= 4) { MFG_POST(4) }
+    else if (ns <= 8) { MFG_POST(8) }
+    else { MFG_POST(16) }
 #undef MFG_POST
+#undef MFG_POST_K
     if (partial) resnorm_final_kernel<<<nc, 32, 0, st>>>(partial, nblk, acc);
     return cudaGetLastError();
 }

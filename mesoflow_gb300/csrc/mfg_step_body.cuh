@@ -488,41 +488,46 @@ __device__ __forceinline__ void clip_body(const Valid& v, const Fab& S, int nspe
 // The step's bookends of one cell after the three RK3 stages, fused
 // (Source/mflo_evolve.cpp:33-58, 470-493, 521-540, 91-112): with chem,
 // phi_old <- phi_new and the chemistry sub-step phi_new = chem(phi_old); the
-// primitive refresh; species clipping when clip.  On return u holds the new
-// state of the cell (every component) and o the state phi_old holds, the
-// operands of the residual norms.  Reads the cell's components once and
-// writes only what changes.
-template <int NS>
-__device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, int j, int k, double dt, bool chem,
-                                          bool clip, bool need_old, double* u, double* o) {
+// primitive refresh; species clipping when clip.  When acc != nullptr the
+// residual-norm terms ((a s_new + b s_old) [* old vfrac for the flow
+// components])^2 of every component are added to acc[n * stride].  Reads the
+// cell's components once and writes only what changes.  With chem, s_old is
+// the incoming s_new, so the components the bookends leave alone (the
+// conserved flow variables and the volume fraction) have the term
+// (a u + b u)^2 = 0 exactly (b = -a): it is added only where u is not finite.
+// CHEM: 0 no sub-step (only_flow), 1 the explicit sub-step of a zero source
+// (no reactions: each species becomes s + 0, which is what the RK3 stages
+// compute then), 2 the sub-step of chem_species.
+template <int NS, int CHEM>
+__device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, int j, int k, double dt, bool clip,
+                                          double a, double b, double* acc, int stride) {
+    constexpr bool chem = CHEM != 0;
     const int ns = c_P.nspec;
-    double spec[NS];
+    double u[NFLO], spec[NS];
 #pragma unroll
     for (int n = 0; n < NFLO; ++n) u[n] = Sn(i, j, k, n);
 #pragma unroll
     for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? Sn(i, j, k, NFLO + s) : 0.0;
+    double o6[TEMP - DENS + 1], os[NS];  // with chem: the old values the bookends change
     if (chem) {
 #pragma unroll
-        for (int n = 0; n < NFLO; ++n) {
-            So(i, j, k, n) = u[n];
-            o[n] = u[n];
+        for (int n = 0; n < NFLO; ++n) So(i, j, k, n) = u[n];
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+            if (s < ns) So(i, j, k, NFLO + s) = spec[s];
+#pragma unroll
+        for (int n = DENS; n <= TEMP; ++n) o6[n - DENS] = u[n];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) os[s] = spec[s];
+        if (CHEM == 2) {
+            double s1[NS];
+            chem_species<NS>(spec, u[TEMP], dt, s1);
+#pragma unroll
+            for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? s1[s] : 0.0;
+        } else {
+#pragma unroll
+            for (int s = 0; s < NS; ++s) spec[s] = add(spec[s], 0.0);
         }
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-            if (s < ns) {
-                So(i, j, k, NFLO + s) = spec[s];
-                o[NFLO + s] = spec[s];
-            }
-        double s1[NS];
-        chem_species<NS>(spec, u[TEMP], dt, s1);
-#pragma unroll
-        for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? s1[s] : 0.0;
-    } else if (need_old) {
-#pragma unroll
-        for (int n = 0; n < NFLO; ++n) o[n] = So(i, j, k, n);
-#pragma unroll
-        for (int s = 0; s < NS; ++s)
-            if (s < ns) o[NFLO + s] = So(i, j, k, NFLO + s);
     }
     const unsigned wrote = prims_cell<NS>(u, spec);
 #pragma unroll
@@ -534,8 +539,26 @@ __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, i
         const double c0 = spec[s];
         if (clip && spec[s] < 0.0) spec[s] = 0.0;
         // stored when the sub-step or the clipping may have changed it
-        if (chem || spec[s] != c0 || (clip && c0 < 0.0)) Sn(i, j, k, NFLO + s) = spec[s];
-        u[NFLO + s] = spec[s];
+        if (chem || (clip && c0 < 0.0)) Sn(i, j, k, NFLO + s) = spec[s];
+    }
+    if (!acc) return;
+    // LinComb then Multiply, rounded as the reference (no contraction)
+    const double vfo = chem ? u[VFRAC] : So(i, j, k, VFRAC);
+#pragma unroll
+    for (int n = 0; n < NFLO; ++n) {
+        const bool changed = n >= DENS && n <= TEMP;
+        if (chem && !changed && isfinite(u[n])) continue;
+        const double on = chem ? o6[changed ? n - DENS : 0] : So(i, j, k, n);
+        double d = add(mul(a, u[n]), mul(b, on));
+        if (n < VFRAC) d = mul(d, vfo);
+        acc[n * stride] += d * d;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        if (s >= ns) continue;
+        const double on = chem ? os[s] : So(i, j, k, NFLO + s);
+        const double d = add(mul(a, spec[s]), mul(b, on));
+        acc[(NFLO + s) * stride] += d * d;
     }
 }
 
