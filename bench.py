@@ -436,6 +436,14 @@ def run_adjoint(a):
         ms = sorted(timed(fn) for _ in range(max(1, a.steps)))
         res[name], mem[name], Js[name] = ms[len(ms) // 2]
     ck = f"adjoint_checkpoint{a.checkpoint}"
+    # per-kernel-kind time of one gradient evaluation (CUDA events per launch)
+    lib.mfg_profile(1)
+    timed(runs[1][1])
+    kk = 32
+    kms, kcnt = (C.c_double * kk)(), (C.c_longlong * kk)()
+    nk = lib.mfg_profile_read(kms, kcnt, kk)
+    lib.mfg_profile(0)
+    kernels = {lib.mfg_profile_name(i).decode(): round(kms[i], 3) for i in range(nk) if kcnt[i]}
     out = {"metric": "adjoint / forward wall-time ratio (gradient of the surface reaction rate)",
            "value": res[ck] / res["forward"], "unit": "x", "higher_is_better": False,
            "n_gpus": 1, "steps": max(1, a.steps), "warmup": a.warmup, "dtype": "f64", "data": "synthetic",
@@ -449,7 +457,8 @@ def run_adjoint(a):
            "ratio_keep_all": res["adjoint_keep_all"] / res["forward"] if "adjoint_keep_all" in res else None,
            "keep_all_skipped": None if "adjoint_keep_all" in res else
            f"every step's intermediates need about {keep_bytes / 1e9:.0f} GB",
-           "gradient_cell_steps_per_s": cells * nsteps / (res[ck] / 1e3)}
+           "gradient_cell_steps_per_s": cells * nsteps / (res[ck] / 1e3),
+           "kernels_ms_checkpoint_run": kernels}
     print(json.dumps(out))
     return 0
 
