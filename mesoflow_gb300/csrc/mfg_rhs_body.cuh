@@ -626,21 +626,26 @@ struct WenoCell {
 // may neither contract nor reorder them differently in the two contexts).
 __device__ __forceinline__ WenoCell weno_cell(double x, double y, double z) {
     WenoCell r;
+    // t = x - 2y + z, tA = 3x - 4y + z, tB = x - 4y + 3z = 4t - tA, q = x - z
     const double t = __dadd_rn(__fma_rn(-2.0, y, x), z);
-    const double kt = __dmul_rn(13.0 / 12.0, __dmul_rn(t, t));
-    const double tA = __dadd_rn(__fma_rn(-4.0, y, __dmul_rn(3.0, x)), z);
-    const double tB = __fma_rn(3.0, z, __fma_rn(-4.0, y, x));
+    const double m4y = __dmul_rn(-4.0, y);
+    const double tA = __dadd_rn(__fma_rn(3.0, x, m4y), z);
+    const double tB = __fma_rn(4.0, t, -tA);
     const double q = __dsub_rn(x, z);
-    const double sA = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, tA), tA, kt));
-    const double sB = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, tB), tB, kt));
-    const double sC = __dadd_rn(kEpsWeno, __fma_rn(__dmul_rn(0.25, q), q, kt));
+    // eps + K1 t^2 + u^2/4 for the three u, with eps folded into the shared term
+    const double kte = __fma_rn(__dmul_rn(13.0 / 12.0, t), t, kEpsWeno);
+    const double sA = __fma_rn(__dmul_rn(0.25, tA), tA, kte);
+    const double sB = __fma_rn(__dmul_rn(0.25, tB), tB, kte);
+    const double sC = __fma_rn(__dmul_rn(0.25, q), q, kte);
     r.dA = __dmul_rn(sA, sA);
     r.dB = __dmul_rn(sB, sB);
     r.dC = __dmul_rn(sC, sC);
-    r.p1 = __fma_rn(11.0, z, __fma_rn(-7.0, y, __dmul_rn(2.0, x)));
-    r.p2 = __fma_rn(2.0, z, __fma_rn(5.0, y, -x));
-    r.p3 = __dsub_rn(__fma_rn(5.0, y, __dmul_rn(2.0, x)), z);
-    r.p4 = __fma_rn(2.0, z, __fma_rn(-7.0, y, __dmul_rn(11.0, x)));
+    // candidates (times 6): 2x - 7y + 11z, -x + 5y + 2z, 2x + 5y - z, 11x - 7y + 2z
+    const double m7y = __dmul_rn(-7.0, y), y5 = __dmul_rn(5.0, y);
+    r.p1 = __fma_rn(11.0, z, __fma_rn(2.0, x, m7y));
+    r.p2 = __fma_rn(2.0, z, __dsub_rn(y5, x));
+    r.p3 = __fma_rn(2.0, x, __dsub_rn(y5, z));
+    r.p4 = __fma_rn(11.0, x, __fma_rn(2.0, z, m7y));
     return r;
 }
 

@@ -412,7 +412,10 @@ __device__ __forceinline__ unsigned prims_cell(double* u, const double* spec) {
     unsigned wrote = 0;
     if (vf == 1.0) {
         const double rho = u[RHO];
-        const double vx = u[RHOU] / rho, vy = u[RHOV] / rho, vz = u[RHOW] / rho;
+        // one Newton-refined reciprocal of the (positive) density for the three
+        // velocities instead of three divisions
+        const double irho = rcp_pos(rho);
+        const double vx = u[RHOU] * irho, vy = u[RHOV] * irho, vz = u[RHOW] * irho;
         const double rhoe = u[RHOE] - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
         const double p = thermo_p<NS>(rhoe, rho, spec);
         u[DENS] = rho;

@@ -46,10 +46,10 @@ def setup(request):
     return case, dt, logA, u_in
 
 
-def oracle_J(case, P, dt, nsteps=NSTEPS):
+def oracle_J(case, P, dt, nsteps=NSTEPS, variant="strict"):
     c2 = copy.copy(case)
     c2.params = P
-    o = OracleLevel(c2)
+    o = OracleLevel(c2, variant=variant)
     for _ in range(nsteps):
         o.advance(dt)
     J = C.c_double()
@@ -57,16 +57,38 @@ def oracle_J(case, P, dt, nsteps=NSTEPS):
     return J.value
 
 
-def fd(fun, logA, u_in):
+def fd(fun, logA, u_in, h=H):
     g = np.zeros(len(logA))
     for r in range(len(logA)):
         a, b = logA.copy(), logA.copy()
-        a[r] += H
-        b[r] -= H
-        g[r] = (fun(a, u_in) - fun(b, u_in)) / (2 * H)
-    hu = H * max(1.0, abs(u_in))
+        a[r] += h
+        b[r] -= h
+        g[r] = (fun(a, u_in) - fun(b, u_in)) / (2 * h)
+    hu = h * max(1.0, abs(u_in))
     gu = (fun(logA, u_in + hu) - fun(logA, u_in - hu)) / (2 * hu)
     return g, gu
+
+
+def test_adjoint_configuration_gradient_matches_fd_of_oracle_h1e6():
+    """The adjoint configuration's check at a size the oracle finishes in
+    seconds: the catalyst block with its seeded sphere pack (seed 5), 32^3 in
+    16^3 boxes, 10 steps with checkpoints every 5 steps (the bounded-memory
+    path), central differences of the oracle's forward (OpenMP build, bitwise
+    the strict one) with h = 1e-6, as in the adjoint benchmark's specification
+    (there 128^3 and 50 steps, beyond what the CPU finishes 18 times)."""
+    case = cases.catalyst(n=32, order=5, max_grid=16, seed=5)
+    nsteps = 10
+    dt = OracleLevel(case, variant="omp").est_timestep()
+    logA = np.array([math.log(case.params.A[r]) for r in range(case.params.nreact)])
+    u_in = case.meta["u_in"]
+    p = ReactionProblem(case, nsteps, dt, checkpoint_every=5)
+    J, gA, gu = p.gradient(logA, u_in)
+    Jo = oracle_J(case, p.params_for(logA, u_in), dt, nsteps, "omp")
+    assert abs(J - Jo) <= 1e-10 * abs(Jo)
+    fA, fu = fd(lambda a, u: oracle_J(case, p.params_for(a, u), dt, nsteps, "omp"), logA, u_in, h=1e-6)
+    print("J", J, "adjoint", gA, gu, "fd", fA, fu)
+    assert close(gA, fA, J), (gA, fA)
+    assert close(gu, fu, J), (gu, fu)
 
 
 def close(adj, ref, J):

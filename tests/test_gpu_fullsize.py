@@ -42,10 +42,14 @@ def test_sod_256_200_steps_matches_oracle_and_exact():
         o.advance(dt)
         g.advance(dt, norms=False)
     sg, so = g.state(), o.state()
+    worst = 0.0
     for comp in range(abi.FLO_NVARS):
         ref = so[comp]
         scale = max(np.linalg.norm(ref), 1e-300)
-        assert np.linalg.norm(sg[comp] - ref) / scale <= 1e-10, comp
+        e = np.linalg.norm(sg[comp] - ref) / scale
+        worst = max(worst, e)
+        assert e <= 1e-10, comp
+    print(f"sod 256x4x4, 200 steps: worst relative L2 against the oracle {worst:.3e}")
     x = (np.arange(256) + 0.5) / 256 - 0.5
     ex = riemann.sample(x, o.time, 1, 0, 1, 0.125, 0, 0.1)
     assert np.abs(sg[abi.RHO][0, 0, :] - ex[0]).mean() < 0.004
