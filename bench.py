@@ -454,6 +454,10 @@ def run_adjoint(a):
            "ms": res, "peak_device_bytes_in_use": mem,
            "J": Js["forward"],
            "J_max_rel_diff_across_modes": max(abs(v - Js["forward"]) for v in Js.values()) / abs(Js["forward"]),
+           "adjoint_pass_over_forward": (res[ck] - res["forward"]) / res["forward"],
+           "adjoint_pass_note": "(gradient - forward) / forward: the recomputation and reverse sweep of the "
+                                "checkpointed steps per forward step, the first forward sweep (which also gives J) "
+                                "taken as the forward",
            "ratio_keep_all": res["adjoint_keep_all"] / res["forward"] if "adjoint_keep_all" in res else None,
            "keep_all_skipped": None if "adjoint_keep_all" in res else
            f"every step's intermediates need about {keep_bytes / 1e9:.0f} GB",

@@ -1426,8 +1426,12 @@ int fwd_step(Work& W, double dt, const Snap* snap, cudaStream_t st) {
                 "forward: phi_old copy");
     for (int stage = 1; stage <= 3; ++stage) {
         ADJ_TRY(launch_fill_patch(W.boxes.data(), W.nbox, W.g, stage == 1 ? 0 : 1, 0.0, st), "forward: fill patch");
-        for (int b = 0; b < W.nbox; ++b)
-            ADJ_TRY(launch_cutcells_box(W.boxes[b], W.g, nullptr, W.d_list, W.d_count, st), "forward: cut cells");
+        // the level-wide pass of mfg_cutcells, else box by box (bitwise the same)
+        const int lv = launch_cutcells_level(W.boxes.data(), W.nbox, W.g, st);
+        if (lv < 0) return MFG_ERR_CUDA;
+        if (lv == 0)
+            for (int b = 0; b < W.nbox; ++b)
+                ADJ_TRY(launch_cutcells_box(W.boxes[b], W.g, nullptr, W.d_list, W.d_count, st), "forward: cut cells");
         for (int b = 0; b < W.nbox; ++b) {
             const mfg_box& x = W.boxes[b];
             if (snap) {
@@ -1440,6 +1444,11 @@ int fwd_step(Work& W, double dt, const Snap* snap, cudaStream_t st) {
             if (snap) snap_views(W, B, *snap, stage, b);  // keep the stage's primitives and face scalars
             ADJ_TRY(launch_rhs_box(B, stage, dt, weno_fast_mode(), st), "forward: right-hand side");
         }
+    }
+    if (!snap) {  // no intermediates kept: the bookends in one pass, as mfg_advance_level
+        for (int b = 0; b < W.nbox; ++b)
+            ADJ_TRY(launch_post_step(W.boxes[b], dt, true, true, nullptr, nullptr, st), "forward: bookends");
+        return MFG_OK;
     }
     for (int b = 0; b < W.nbox; ++b) {
         const mfg_box& x = W.boxes[b];

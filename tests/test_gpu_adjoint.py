@@ -75,7 +75,12 @@ def test_adjoint_configuration_gradient_matches_fd_of_oracle_h1e6():
     16^3 boxes, 10 steps with checkpoints every 5 steps (the bounded-memory
     path), central differences of the oracle's forward (OpenMP build, bitwise
     the strict one) with h = 1e-6, as in the adjoint benchmark's specification
-    (there 128^3 and 50 steps, beyond what the CPU finishes 18 times)."""
+    (there 128^3 and 50 steps, beyond what the CPU finishes 18 times).
+
+    Tolerance 1e-6 |g| + 3e-8 |J|: with h = 1e-6 the central difference
+    carries the rounding noise of J between the perturbed runs (about 1e-14 of
+    J after 10 steps of this case) divided by h, about 1e-8 |J|; the gradients
+    of the reactions that carry J agree to 1e-6 relative."""
     case = cases.catalyst(n=32, order=5, max_grid=16, seed=5)
     nsteps = 10
     dt = OracleLevel(case, variant="omp").est_timestep()
@@ -87,12 +92,13 @@ def test_adjoint_configuration_gradient_matches_fd_of_oracle_h1e6():
     assert abs(J - Jo) <= 1e-10 * abs(Jo)
     fA, fu = fd(lambda a, u: oracle_J(case, p.params_for(a, u), dt, nsteps, "omp"), logA, u_in, h=1e-6)
     print("J", J, "adjoint", gA, gu, "fd", fA, fu)
-    assert close(gA, fA, J), (gA, fA)
-    assert close(gu, fu, J), (gu, fu)
+    print("worst |adjoint - fd| / |J|", max(np.max(np.abs(gA - fA)), abs(gu - fu)) / abs(J))
+    assert close(gA, fA, J, 3e-8), (gA, fA)
+    assert close(gu, fu, J, 3e-8), (gu, fu)
 
 
-def close(adj, ref, J):
-    return np.all(np.abs(np.asarray(adj) - np.asarray(ref)) <= RTOL * np.abs(ref) + ATOL_J * abs(J))
+def close(adj, ref, J, atol_j=ATOL_J):
+    return np.all(np.abs(np.asarray(adj) - np.asarray(ref)) <= RTOL * np.abs(ref) + atol_j * abs(J))
 
 
 def test_adjoint_forward_is_the_plain_step(setup):
