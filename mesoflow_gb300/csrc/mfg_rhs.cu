@@ -80,8 +80,12 @@ __global__ void __launch_bounds__(TPB) face_split_kernel(RhsBox B) {
 }
 // The direction is the block's (blockIdx.y), uniform as in face_kernel, so
 // the compiler forms the same multiply-adds in both.
+// 128-thread blocks at 5 per SM (96 registers): 20 resident warps instead of
+// the 16 that 256-thread blocks at 116 registers give; the FP64-bound pass
+// issues 3% faster.
+constexpr int LIST_TPB = 128;
 template <int NS>
-__global__ void __launch_bounds__(TPB) face_list_kernel(RhsBox B) {
+__global__ void __launch_bounds__(LIST_TPB, 5) face_list_kernel(RhsBox B) {
     const int d = blockIdx.y;
     const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w < B.fcount[d]) face_body<NS>(B, d, B.flist[face_list_off(B, d) + w]);
@@ -133,7 +137,7 @@ cudaError_t launch_box_ns(const RhsBox& B, int stage, double dt, bool fast, cuda
         cudaMemsetAsync(B.fcount, 0, 3 * sizeof(unsigned), st);
         ProfScope ps(K_FACE, st, 2);
         face_split_kernel<NS><<<dim3(blocks_for(nfmax), 3), TPB, 0, st>>>(B);
-        face_list_kernel<NS><<<dim3(blocks_for(nfmax), 3), TPB, 0, st>>>(B);
+        face_list_kernel<NS><<<dim3((unsigned)((nfmax + LIST_TPB - 1) / LIST_TPB), 3), LIST_TPB, 0, st>>>(B);
     }
     for (int d = 0; d < 3 && !split; ++d) {
         int64_t nf = 1;
