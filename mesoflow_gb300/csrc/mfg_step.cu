@@ -66,33 +66,49 @@ __global__ void resnorm_kernel(Valid v, Fab Sn, Fab So, double a, double b, doub
 // <- phi_new and the chemistry sub-step when chem, primitive refresh, species
 // clipping when clip) and, when partial != nullptr, the block partial sums of
 // the residual norms ((s_new - s_old)/dt, flow components scaled by the old
-// volume fraction).  Each thread adds its cells' terms to its own slot of a
-// shared-memory table ([component][thread]); one warp per component then sums
-// the slots in a fixed order, so the partials are deterministic.
+// volume fraction).  Each thread keeps one running sum per component in
+// registers (with the chemistry sub-step, only the components the bookends
+// change can be non-zero); the block then sums them by warp shuffles and one
+// warp adds the warps' sums in a fixed order, so the partials are
+// deterministic.
 constexpr int PTPB = 128;
 
-template <int NS, int CHEM>
+template <int NS, int CHEM, bool NORMS>
 __global__ void __launch_bounds__(PTPB) post_step_kernel(Valid v, Fab So, Fab Sn, double dt, int clip, double a,
                                                          double b, double* partial, int nblk) {
-    extern __shared__ double sacc[];  // [ncomp][PTPB] when partial
+    constexpr int NM = NFLO + NS;
     const int N = NFLO + c_P.nspec;
-    double* mine = partial ? sacc + threadIdx.x : nullptr;
-    if (partial)
-        for (int n = 0; n < N; ++n) mine[n * PTPB] = 0.0;
+    double acc[NM];
+#pragma unroll
+    for (int n = 0; n < NM; ++n) acc[n] = 0.0;
+    bool nonfinite = false;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < v.n; t += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of(v, t, i, j, k);
-        post_cell<NS, CHEM>(So, Sn, i, j, k, dt, clip != 0, a, b, mine, PTPB);
+        post_cell<NS, CHEM, NORMS>(So, Sn, i, j, k, dt, clip != 0, a, b, acc, nonfinite);
     }
-    if (!partial) return;
-    __syncthreads();
+    if (!NORMS) return;
+    const int any_nonfinite = __syncthreads_or(nonfinite ? 1 : 0);
+    __shared__ double ws[PTPB / 32][NM];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int n = warp; n < N; n += PTPB / 32) {
-        double x = 0.0;
 #pragma unroll
-        for (int q = 0; q < PTPB / 32; ++q) x += sacc[n * PTPB + q * 32 + lane];
+    for (int n = 0; n < NM; ++n) {
+        if (CHEM != 0 && !(n >= DENS && n <= TEMP) && n < NFLO) continue;  // zero in every cell
+        double x = acc[n];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) partial[(int64_t)n * nblk + blockIdx.x] = x;
+        if (lane == 0) ws[warp][n] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        const int n = threadIdx.x;
+        double x;
+        if (CHEM != 0 && !(n >= DENS && n <= TEMP) && n < NFLO) {
+            x = any_nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
+        } else {
+            x = 0.0;
+            for (int w = 0; w < PTPB / 32; ++w) x += ws[w][n];
+        }
+        partial[(int64_t)n * nblk + blockIdx.x] = x;
     }
 }
 
@@ -234,13 +250,18 @@ cudaError_t launch_post_step(const mfg_box& b, double dt, bool chem, bool clip, 
     // one cell per thread up to 1024 blocks, then a grid-stride loop
     const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (v.n + PTPB - 1) / PTPB));
     const double a = 1.0 / dt, bb = -1.0 / dt;
-    const size_t smem = partial ? (size_t)nc * PTPB * sizeof(double) : 0;
+    const size_t smem = 0;
     const DevParams& P = c_host_params();
     // the sub-step of a zero source (no reactions, explicit integrator) is s + 0
     const int kind = !chem ? 0 : (P.chem_kind == 0 && (!P.chem_on || P.nreact == 0)) ? 1 : 2;
     ProfScope ps(K_POST, st, partial ? 2 : 1);
-#define MFG_POST_K(NSB, K) post_step_kernel<NSB, K><<<nblk, PTPB, smem, st>>>(v, make_fab(b.s_old), \
-                                                   make_fab(b.s_new), dt, clip, a, bb, partial, nblk)
+#define MFG_POST_K(NSB, K)                                                                               \
+    if (partial)                                                                                         \
+        post_step_kernel<NSB, K, true><<<nblk, PTPB, smem, st>>>(v, make_fab(b.s_old), make_fab(b.s_new), dt, \
+                                                                 clip, a, bb, partial, nblk);            \
+    else                                                                                                 \
+        post_step_kernel<NSB, K, false><<<nblk, PTPB, smem, st>>>(v, make_fab(b.s_old), make_fab(b.s_new), dt, \
+                                                                  clip, a, bb, partial, nblk)
 #define MFG_POST(NSB)                     \
     if (kind == 0) MFG_POST_K(NSB, 0);    \
     else if (kind == 1) MFG_POST_K(NSB, 1); \

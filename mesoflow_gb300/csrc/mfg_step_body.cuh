@@ -491,19 +491,20 @@ __device__ __forceinline__ void clip_body(const Valid& v, const Fab& S, int nspe
 // The step's bookends of one cell after the three RK3 stages, fused
 // (Source/mflo_evolve.cpp:33-58, 470-493, 521-540, 91-112): with chem,
 // phi_old <- phi_new and the chemistry sub-step phi_new = chem(phi_old); the
-// primitive refresh; species clipping when clip.  When acc != nullptr the
+// primitive refresh; species clipping when clip.  With NORMS the
 // residual-norm terms ((a s_new + b s_old) [* old vfrac for the flow
-// components])^2 of every component are added to acc[n * stride].  Reads the
+// components])^2 of every component are added to acc[n].  Reads the
 // cell's components once and writes only what changes.  With chem, s_old is
 // the incoming s_new, so the components the bookends leave alone (the
 // conserved flow variables and the volume fraction) have the term
-// (a u + b u)^2 = 0 exactly (b = -a): it is added only where u is not finite.
+// (a u + b u)^2 = 0 exactly (b = -a), NaN where u is not finite: only
+// nonfinite is raised for them.
 // CHEM: 0 no sub-step (only_flow), 1 the explicit sub-step of a zero source
 // (no reactions: each species becomes s + 0, which is what the RK3 stages
 // compute then), 2 the sub-step of chem_species.
-template <int NS, int CHEM>
+template <int NS, int CHEM, bool NORMS>
 __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, int j, int k, double dt, bool clip,
-                                          double a, double b, double* acc, int stride) {
+                                          double a, double b, double* acc, bool& nonfinite) {
     constexpr bool chem = CHEM != 0;
     const int ns = c_P.nspec;
     double u[NFLO], spec[NS];
@@ -544,24 +545,28 @@ __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, i
         // stored when the sub-step or the clipping may have changed it
         if (chem || (clip && c0 < 0.0)) Sn(i, j, k, NFLO + s) = spec[s];
     }
-    if (!acc) return;
-    // LinComb then Multiply, rounded as the reference (no contraction)
+    if (!NORMS) return;
+    // LinComb then Multiply, rounded as the reference (no contraction); acc
+    // holds one running sum per component in registers
     const double vfo = chem ? u[VFRAC] : So(i, j, k, VFRAC);
 #pragma unroll
     for (int n = 0; n < NFLO; ++n) {
         const bool changed = n >= DENS && n <= TEMP;
-        if (chem && !changed && isfinite(u[n])) continue;
+        if (chem && !changed) {  // (a u + b u)^2 = 0 unless u is not finite
+            nonfinite |= !isfinite(u[n]);
+            continue;
+        }
         const double on = chem ? o6[changed ? n - DENS : 0] : So(i, j, k, n);
         double d = add(mul(a, u[n]), mul(b, on));
         if (n < VFRAC) d = mul(d, vfo);
-        acc[n * stride] += d * d;
+        acc[n] += d * d;
     }
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         if (s >= ns) continue;
         const double on = chem ? os[s] : So(i, j, k, NFLO + s);
         const double d = add(mul(a, spec[s]), mul(b, on));
-        acc[(NFLO + s) * stride] += d * d;
+        acc[NFLO + s] += d * d;
     }
 }
 
