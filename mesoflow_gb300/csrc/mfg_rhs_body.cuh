@@ -284,10 +284,14 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             const double HL = gfL * (pL * irL) + 0.5 * kL;
             const double HR = gfR * (pR * irR) + 0.5 * kR;
             const double rho_half = 0.5 * (rL + rR);
+            // a_hat = a*^2 / max(a*, |v|): a* itself where a* >= |v| (subsonic
+            // side, a*^2/a* to within an ulp), one reciprocal otherwise
             double as2 = afL * HL;
-            const double ahL = as2 * rcp_pos(max_nonneg(sqrt(as2), fabs(vL)));
+            double sq = sqrt(as2);
+            const double ahL = nonneg_ge(sq, fabs(vL)) ? sq : as2 * rcp_pos(fabs(vL));
             as2 = afR * HR;
-            const double ahR = as2 * rcp_pos(max_nonneg(sqrt(as2), fabs(vR)));
+            sq = sqrt(as2);
+            const double ahR = nonneg_ge(sq, fabs(vR)) ? sq : as2 * rcp_pos(fabs(vR));
             const double ah = min_nonneg(ahL, ahR);
             const double iah = rcp_pos(ah);
             const double ML = vL * iah, MR = vR * iah;
@@ -313,7 +317,9 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double* V0 = S.p + VELX * S.ns;
         const double* V1 = S.p + VELY * S.ns;
         const double* V2 = S.p + VELZ * S.ns;
-        const double ids = B.idx[d], ih1 = 0.5 * B.idx[t1], ih2 = 0.5 * B.idx[t2];
+        // transverse derivatives (0.5 (a + b) - 0.5 (c + d)) / (2 dx) formed as
+        // ((a + b) - (c + d)) / (4 dx)
+        const double ids = B.idx[d], iq1 = 0.25 * B.idx[t1], iq2 = 0.25 * B.idx[t2];
         // Only the stress row of the face normal is needed: tau_{d a} uses the
         // normal derivatives of all three velocities, the two transverse
         // derivatives of the normal velocity, and the divergence's two other
@@ -322,10 +328,10 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double* Vt1 = (t1 == 0) ? V0 : (t1 == 1) ? V1 : V2;
         const double* Vt2 = (t2 == 0) ? V0 : (t2 == 1) ? V1 : V2;
         const double gn0 = (V0[oR] - V0[oL]) * ids, gn1 = (V1[oR] - V1[oL]) * ids, gn2 = (V2[oR] - V2[oL]) * ids;
-        const double d_t1 = (0.5 * (Vd[oL + st1] + Vd[oR + st1]) - 0.5 * (Vd[oL - st1] + Vd[oR - st1])) * ih1;
-        const double d_t2 = (0.5 * (Vd[oL + st2] + Vd[oR + st2]) - 0.5 * (Vd[oL - st2] + Vd[oR - st2])) * ih2;
-        const double t1_t1 = (0.5 * (Vt1[oL + st1] + Vt1[oR + st1]) - 0.5 * (Vt1[oL - st1] + Vt1[oR - st1])) * ih1;
-        const double t2_t2 = (0.5 * (Vt2[oL + st2] + Vt2[oR + st2]) - 0.5 * (Vt2[oL - st2] + Vt2[oR - st2])) * ih2;
+        const double d_t1 = ((Vd[oL + st1] + Vd[oR + st1]) - (Vd[oL - st1] + Vd[oR - st1])) * iq1;
+        const double d_t2 = ((Vd[oL + st2] + Vd[oR + st2]) - (Vd[oL - st2] + Vd[oR - st2])) * iq2;
+        const double t1_t1 = ((Vt1[oL + st1] + Vt1[oR + st1]) - (Vt1[oL - st1] + Vt1[oR - st1])) * iq1;
+        const double t2_t2 = ((Vt2[oL + st2] + Vt2[oR + st2]) - (Vt2[oL - st2] + Vt2[oR - st2])) * iq2;
         // du/dx, dv/dy, dw/dz: the normal derivative along d, else the transverse one
         const double dudx = (d == 0) ? gn0 : (t1 == 0) ? t1_t1 : t2_t2;
         const double dvdy = (d == 1) ? gn1 : (t1 == 1) ? t1_t1 : t2_t2;
@@ -364,6 +370,9 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const int64_t qo = O.off(f.i, f.j, f.k);
         const Fab& U = B.uflux[d];
         const int64_t qu = U.p ? U.off(f.i, f.j, f.k) : 0;
+        // AUSM+-up mass-flux weights of the face, the wave speed folded in:
+        // fh = (M/2 (fL + fR) - |M|/2 (fR - fL)) a_half per component
+        const double cmh = (0.5 * fs[FS_MH]) * fs[FS_LAMBDA], cmod = (0.5 * fs[FS_MODM]) * fs[FS_LAMBDA];
 #pragma unroll
         for (int c = 0; c < NCONS + NS; ++c) {
             if (c >= NCONS + P.nspec) break;
@@ -375,7 +384,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
                     fL = uL[c] + fs[FS_PL];
                     fR = uR[c] + fs[FS_PR];
                 }
-                double fh = ((0.5 * fs[FS_MH]) * (fL + fR) - (0.5 * fs[FS_MODM]) * (fR - fL)) * fs[FS_LAMBDA];
+                double fh = cmh * (fL + fR) - cmod * (fR - fL);
                 if (c == 1 + d) fh += fs[FS_PH];
                 F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
                 if (c >= RHOU && c <= RHOW) F -= fs[FS_VIS + c - 1];
