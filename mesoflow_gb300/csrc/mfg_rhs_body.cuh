@@ -571,8 +571,9 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
         const int64_t ox = Fx.off(x.i, x.j, x.k) + c * Fx.ns;
         const int64_t oy = Fy.off(x.i, x.j, x.k) + c * Fy.ns;
         const int64_t oz = Fz.off(x.i, x.j, x.k) + c * Fz.ns;
-        ds = ((Fx.p[ox] - Fx.p[ox + 1]) * B.idx[0] + (Fy.p[oy] - Fy.p[oy + Fy.js]) * B.idx[1]) +
-             (Fz.p[oz] - Fz.p[oz + Fz.ks]) * B.idx[2];
+        // explicit FMAs: every compiled copy of this body rounds the same way
+        ds = __fma_rn(Fz.p[oz] - Fz.p[oz + Fz.ks], B.idx[2],
+                      __fma_rn(Fy.p[oy] - Fy.p[oy + Fy.js], B.idx[1], mul(Fx.p[ox] - Fx.p[ox + 1], B.idx[0])));
         ds = plus_zero(ds);  // + source (compute_fluid_source is zero)
     }
     const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
@@ -587,17 +588,20 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
     }
     if (is_nan(ds)) raise_status(MFG_STATUS_NAN);
     if (B.dsdt.p) B.dsdt(x.i, x.j, x.k, n) = ds;
+    // The stage algebra of the advected components with fused multiply-adds
+    // (one rounding less per product than the reference's separate ones, 3
+    // instead of 5 FP64 operations in stages 2 and 3); the components without
+    // a flux above keep the reference's rounding, so the volume fraction and
+    // the cut-cell classification it drives evolve exactly as there.
     if (stage == 1) {
-        B.snew(x.i, x.j, x.k, n) = add(B.sb(x.i, x.j, x.k, n), mul(dt, ds));
+        B.snew(x.i, x.j, x.k, n) = __fma_rn(dt, ds, B.sb(x.i, x.j, x.k, n));
     } else if (stage == 2) {
-        double v = B.snew(x.i, x.j, x.k, n);
-        v = add(v, mul(dt, ds));
-        v = add(v, mul(3.0, B.sold(x.i, x.j, x.k, n)));
+        double v = __fma_rn(dt, ds, B.snew(x.i, x.j, x.k, n));
+        v = __fma_rn(3.0, B.sold(x.i, x.j, x.k, n), v);
         B.snew(x.i, x.j, x.k, n) = mul(v, 0.25);
     } else if (stage == 3) {
-        double v = B.snew(x.i, x.j, x.k, n);
-        v = add(v, mul(dt, ds));
-        v = add(B.sold(x.i, x.j, x.k, n), mul(2.0, v));
+        double v = __fma_rn(dt, ds, B.snew(x.i, x.j, x.k, n));
+        v = __fma_rn(2.0, v, B.sold(x.i, x.j, x.k, n));
         B.snew(x.i, x.j, x.k, n) = mul(v, kThird);
     }
 }
