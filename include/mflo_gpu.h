@@ -293,6 +293,21 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom,
                       double time, double dt, int only_flow, int clip,
                       double* resnorms, void* stream);
 
+/* mfg_advance_level for a driver whose state FABs live in host memory (the
+ * reference's CPU build: its per-box MFIter bodies of mflo_evolve.cpp:251-318
+ * read host Array4s).  h_state[b] is a host view with the layout of
+ * boxes[b].s_new (same strides, begin, end and ncomp; else MFG_ERR_ARG); it
+ * holds phi_new on entry and receives it on return.  Each box's view is copied
+ * in on the stream before the step, and copied back on an internal copy
+ * stream as soon as that box's last kernels (its stage-3 update and bookends)
+ * are done, so the copies back overlap the later boxes' compute.  Results are
+ * bitwise those of copy-in + mfg_advance_level + copy-out.  Pinned
+ * (page-locked) host memory moves at link speed; pageable memory works but is
+ * staged by the driver.  Synchronizes the stream. */
+int mfg_advance_level_host(const mfg_box* boxes, int nbox, const mfg_geom* geom,
+                           double time, double dt, int only_flow, int clip,
+                           const mfg_array4* h_state, double* resnorms, void* stream);
+
 /* Selects the WENO5 nonlinear-weight normalisation: fast != 0 uses one
  * division per reconstructed value (default), 0 follows the reference's
  * four reciprocals (flux_schemes.H:407-414) operation for operation. */

@@ -99,6 +99,8 @@ SIGNATURES = [
     ("mfg_est_timestep", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.POINTER(C.c_double), _VP]),
     ("mfg_advance_level", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.POINTER(C.c_double), _VP]),
+    ("mfg_advance_level_host", C.c_int, [_BP, C.c_int, _GP, C.c_double, C.c_double, C.c_int, C.c_int,
+                                         C.POINTER(Array4), C.POINTER(C.c_double), _VP]),
     ("mfg_set_weno_mode", C.c_int, [C.c_int]),
     ("mfg_set_cutcell_cache", C.c_int, [C.c_int]),
     ("mfg_set_face_compaction", C.c_int, [C.c_int]),

@@ -46,6 +46,50 @@ cudaError_t pool_reserve(size_t bytes, cudaStream_t st) {
     return cudaSuccess;
 }
 
+// Copy stream and event of the host-buffer level step, created on first use
+// for the device current then (re-created if the current device changed).
+struct CopyStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    int dev = -1;
+} g_copy;
+
+void copy_stream_release() {
+    if (g_copy.s) cudaStreamDestroy(g_copy.s);
+    if (g_copy.ev) cudaEventDestroy(g_copy.ev);
+    g_copy = CopyStream();
+}
+
+cudaError_t copy_stream(cudaStream_t* s, cudaEvent_t* ev) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (!g_copy.s || g_copy.dev != dev) {
+        copy_stream_release();
+        if ((e = cudaStreamCreateWithFlags(&g_copy.s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&g_copy.ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+        g_copy.dev = dev;
+    }
+    *s = g_copy.s;
+    *ev = g_copy.ev;
+    return cudaSuccess;
+}
+
+// Doubles from a view's first element to its last (the memory one copy of
+// the whole view moves).
+size_t view_span_doubles(const mfg_array4& a) {
+    return (size_t)((int64_t)(a.ncomp - 1) * a.nstride + (int64_t)(a.end[2] - a.begin[2] - 1) * a.kstride +
+                    (int64_t)(a.end[1] - a.begin[1] - 1) * a.jstride + (a.end[0] - a.begin[0]));
+}
+
+bool same_layout(const mfg_array4& h, const mfg_array4& d) {
+    if (!h.p || h.jstride != d.jstride || h.kstride != d.kstride || h.nstride != d.nstride || h.ncomp != d.ncomp)
+        return false;
+    for (int e = 0; e < 3; ++e)
+        if (h.begin[e] != d.begin[e] || h.end[e] != d.end[e]) return false;
+    return true;
+}
+
 int ncomp_total() { return NFLO + g_hp.nspec; }
 int ncomp_adv() { return NCONS + g_hp.nspec; }
 
@@ -221,6 +265,7 @@ int mfg_init(const mfg_params* p) {
         h.g_gm1 = p->gamma_single / (p->gamma_single - 1.0);
         h.astar_fac = (2.0 * (p->gamma_single - 1.0)) / (p->gamma_single + 1.0);
         h.gm1_single = p->gamma_single - 1.0;
+        h.inv_gas_R = 1.0 / p->gas_R;
     }
     h.visc_mode = p->visc_mode;
     h.cond_mode = p->cond_mode;
@@ -283,6 +328,7 @@ int mfg_finalize(void) {
     fill_release();
     cutcache_release();
     noalloc_forget();
+    copy_stream_release();
     g_ready = false;
     return MFG_OK;
 }
@@ -472,38 +518,70 @@ int mfg_est_timestep(const mfg_box* boxes, int nbox, const mfg_geom* geom, doubl
 // One coarse step of a single level: the swap, three RK3 stages (fill patch,
 // cut cells, fused RHS + stage algebra), the Strang chemistry sub-step, the
 // primitive refresh, species clipping and residual norms
-// (Source/mflo_evolve.cpp:251-318, 470-493, 33-58).
-int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, double time, double dt, int only_flow,
-                      int clip, double* resnorms, void* stream) {
-    int rc = check_boxes(boxes, nbox, true, false, true, true);
-    if (rc) return rc;
-    if (!geom) return MFG_ERR_ARG;
-    cudaStream_t st = (cudaStream_t)stream;
+// (Source/mflo_evolve.cpp:251-318, 470-493, 33-58).  The bookends of box b
+// run right after its stage-3 update (the box's state is still in L2, and no
+// other box's stage 3 reads it: every box reads its own filled Sborder), in
+// box order, so the residual-norm sums run in the same order as a separate
+// pass.  With h_state, each box's phi_new is copied in from the host first and
+// copied back on the copy stream as soon as its bookends are done.
+static int advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, double time, double dt,
+                         int only_flow, int clip, double* resnorms, const mfg_array4* h_state, cudaStream_t st) {
+    int rc;
     const int N = ncomp_total();
+    size_t need = 0;
+    for (int b = 0; b < nbox; ++b) {
+        int n[3];
+        for (int d = 0; d < 3; ++d) n[d] = boxes[b].hi[d] - boxes[b].lo[d] + 1;
+        need = std::max(need, rhs_scratch_doubles(n));
+    }
+    const size_t npart = (size_t)N * 1024;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (h_state) {
+        if (copy_stream(&cs, &ev) != cudaSuccess) return MFG_ERR_CUDA;
+        for (int b = 0; b < nbox; ++b)
+            if (cudaMemcpyAsync(boxes[b].s_new.p, h_state[b].p, view_span_doubles(boxes[b].s_new) * sizeof(double),
+                                cudaMemcpyHostToDevice, st) != cudaSuccess)
+                return MFG_ERR_CUDA;
+    }
     Fab none;
     memset(&none, 0, sizeof(none));
     for (int b = 0; b < nbox; ++b)  // phi_old <- phi_new (std::swap of the reference)
         if (launch_axpy_valid(boxes[b], make_fab(boxes[b].s_old), none, 0.0, true, make_fab(boxes[b].s_new), N, st) !=
             cudaSuccess)
             return MFG_ERR_CUDA;
+    double* acc = nullptr;
     for (int stage = 1; stage <= 3; ++stage) {
-        if ((rc = mfg_fill_patch(boxes, nbox, geom, stage == 1 ? 0 : 1, stage == 1 ? time : time + dt, stream)))
+        if ((rc = mfg_fill_patch(boxes, nbox, geom, stage == 1 ? 0 : 1, stage == 1 ? time : time + dt, st)))
             return rc;
-        if ((rc = mfg_cutcells(boxes, nbox, geom, time, stream))) return rc;
-        if ((rc = run_rhs(boxes, nbox, geom, stage, dt, st))) return rc;
+        if ((rc = mfg_cutcells(boxes, nbox, geom, time, st))) return rc;
+        // the pool after the cut-cell pass (whose per-box form uses it too):
+        // RHS scratch first, then the residual-norm partials and sums, which
+        // must survive the later boxes' RHS launches of stage 3
+        if (pool_reserve((need + npart + N) * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
+        double* scratch = reinterpret_cast<double*>(g_pool.p);
+        double* part = (resnorms && stage == 3) ? scratch + need : nullptr;
+        acc = part ? part + npart : nullptr;
+        if (acc && cudaMemsetAsync(acc, 0, N * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
+        for (int b = 0; b < nbox; ++b) {
+            RhsBox B = make_rhs_box(boxes[b], *geom, scratch);
+            if (launch_rhs_box(B, stage, dt, g_fast_weno, st) != cudaSuccess) return MFG_ERR_CUDA;
+            if (stage < 3) continue;
+            // the bookends in one pass: phi_old <- phi_new and the chemistry
+            // sub-step (unless only_flow), primitive refresh, clipping, norms
+            if (launch_post_step(boxes[b], dt, !only_flow, clip != 0, part, acc, st) != cudaSuccess)
+                return MFG_ERR_CUDA;
+            if (h_state) {
+                if (cudaEventRecord(ev, st) != cudaSuccess || cudaStreamWaitEvent(cs, ev, 0) != cudaSuccess ||
+                    cudaMemcpyAsync(h_state[b].p, boxes[b].s_new.p,
+                                    view_span_doubles(boxes[b].s_new) * sizeof(double), cudaMemcpyDeviceToHost,
+                                    cs) != cudaSuccess)
+                    return MFG_ERR_CUDA;
+            }
+        }
     }
-    // the bookends in one pass per box: phi_old <- phi_new and the chemistry
-    // sub-step (unless only_flow), primitive refresh, clipping, residual norms
-    double *part = nullptr, *acc = nullptr;
-    const size_t npart = (size_t)N * 1024;
-    if (resnorms) {
-        if (pool_reserve((npart + N) * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
-        part = reinterpret_cast<double*>(g_pool.p);
-        acc = part + npart;
-        if (cudaMemsetAsync(acc, 0, N * sizeof(double), st) != cudaSuccess) return MFG_ERR_CUDA;
-    }
-    for (int b = 0; b < nbox; ++b)
-        if (launch_post_step(boxes[b], dt, !only_flow, clip != 0, part, acc, st) != cudaSuccess) return MFG_ERR_CUDA;
+    if (h_state && (cudaEventRecord(ev, cs) != cudaSuccess || cudaStreamWaitEvent(st, ev, 0) != cudaSuccess))
+        return MFG_ERR_CUDA;
     std::vector<double> hn(resnorms ? N : 0);
     if (resnorms && cudaMemcpyAsync(hn.data(), acc, N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return MFG_ERR_CUDA;
@@ -515,6 +593,24 @@ int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, doub
     if (v & MFG_STATUS_NEG_PRESSURE) return MFG_ERR_NEG_PRESSURE;
     if (v & MFG_STATUS_NAN) return MFG_ERR_NAN;
     return MFG_OK;
+}
+
+int mfg_advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, double time, double dt, int only_flow,
+                      int clip, double* resnorms, void* stream) {
+    int rc = check_boxes(boxes, nbox, true, false, true, true);
+    if (rc) return rc;
+    if (!geom) return MFG_ERR_ARG;
+    return advance_level(boxes, nbox, geom, time, dt, only_flow, clip, resnorms, nullptr, (cudaStream_t)stream);
+}
+
+int mfg_advance_level_host(const mfg_box* boxes, int nbox, const mfg_geom* geom, double time, double dt,
+                           int only_flow, int clip, const mfg_array4* h_state, double* resnorms, void* stream) {
+    int rc = check_boxes(boxes, nbox, true, false, true, true);
+    if (rc) return rc;
+    if (!geom || !h_state) return MFG_ERR_ARG;
+    for (int b = 0; b < nbox; ++b)
+        if (!same_layout(h_state[b], boxes[b].s_new)) return MFG_ERR_ARG;
+    return advance_level(boxes, nbox, geom, time, dt, only_flow, clip, resnorms, h_state, (cudaStream_t)stream);
 }
 
 int mfg_set_cutcell_cache(int enable) {

@@ -42,7 +42,7 @@ struct DevParams {
     // face coefficients of constant transport: harmonic_mean(g, g), evaluated once
     double visc_hm, cond_hm, diff_hm[MAXS];
     // gamma/(gamma-1) and 2(gamma-1)/(gamma+1) of the mass-single family
-    double g_gm1, astar_fac, gm1_single;
+    double g_gm1, astar_fac, gm1_single, inv_gas_R;
     int order_hyp, do_ns, species_in_solid, conj_ht;
     double dissfactor, solid_temp, cfl;
     int chem_on, nreact;
@@ -160,6 +160,10 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
     return __longlong_as_double(ia < ib ? ia : ib);
 }
 __device__ __forceinline__ double pos_part(double x) { return is_positive(x) ? x : 0.0; }  // max(x, 0)
+__device__ __forceinline__ bool is_negative(double x) {  // x < 0 (false for -0 and NaN)
+    const long long b = __double_as_longlong(x), m = b & 0x7FFFFFFFFFFFFFFFLL;
+    return b < 0 && m != 0 && m <= 0x7FF0000000000000LL;
+}
 __device__ __forceinline__ bool is_nan(double x) {
     return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
 }

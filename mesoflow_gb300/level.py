@@ -110,6 +110,22 @@ class Level:
         self._desc = arr
         return arr
 
+    def host_views(self, host):
+        """ctypes array of mfg_array4: each box's phi_new layout over the host
+        array host[b] (same shape as s_new[b], C-contiguous; pinned for link
+        speed), for mfg_advance_level_host."""
+        desc = self.descriptors()
+        arr = (abi.Array4 * len(self.boxes))()
+        for b, h in enumerate(host):
+            if tuple(h.shape) != tuple(self.s_new[b].shape):
+                raise ValueError(f"host array {b}: shape {tuple(h.shape)}, phi_new {tuple(self.s_new[b].shape)}")
+            contiguous = h.flags.c_contiguous if isinstance(h, np.ndarray) else h.is_contiguous()
+            if not contiguous:
+                raise ValueError(f"host array {b} is not C-contiguous")
+            arr[b] = desc[b].s_new
+            arr[b].p = h.ctypes.data if isinstance(h, np.ndarray) else h.data_ptr()
+        return arr
+
     # -- whole-level state -----------------------------------------------------
     def set_state(self, full, domain_lo=(0, 0, 0), which="new"):
         """Copies a domain array (ncomp, Z, Y, X) into every box's phi_new (or phi_old)."""
