@@ -371,8 +371,11 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const Fab& U = B.uflux[d];
         const int64_t qu = U.p ? U.off(f.i, f.j, f.k) : 0;
         // AUSM+-up mass-flux weights of the face, the wave speed folded in:
-        // fh = (M/2 (fL + fR) - |M|/2 (fR - fL)) a_half per component
+        // fh = (M/2 (fL + fR) - |M|/2 (fR - fL)) a_half per component, as
+        // wL fL + wR fR with wL = (M + |M|) a_half / 2, wR = (M - |M|) a_half / 2
+        // (two FP64 operations per component instead of four)
         const double cmh = (0.5 * fs[FS_MH]) * fs[FS_LAMBDA], cmod = (0.5 * fs[FS_MODM]) * fs[FS_LAMBDA];
+        const double wL = cmh + cmod, wR = cmh - cmod;
 #pragma unroll
         for (int c = 0; c < NCONS + NS; ++c) {
             if (c >= NCONS + P.nspec) break;
@@ -384,7 +387,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
                     fL = uL[c] + fs[FS_PL];
                     fR = uR[c] + fs[FS_PR];
                 }
-                double fh = cmh * (fL + fR) - cmod * (fR - fL);
+                double fh = fma(wR, fR, wL * fL);
                 if (c == 1 + d) fh += fs[FS_PH];
                 F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
                 if (c >= RHOU && c <= RHOW) F -= fs[FS_VIS + c - 1];

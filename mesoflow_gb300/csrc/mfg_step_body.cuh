@@ -410,10 +410,12 @@ __device__ __forceinline__ unsigned prims_cell(double* u, const double* spec) {
     const DevParams& P = c_P;
     const double vf = u[VFRAC];
     unsigned wrote = 0;
-    if (vf == 1.0) {
+    // the volume-fraction, pressure and finiteness tests of the bookends run
+    // on the integer pipe (the FP64 pipe bounds this kernel)
+    if (is_one(vf)) {
         const double rho = u[RHO];
         // one Newton-refined reciprocal of the (positive) density for the three
-        // velocities instead of three divisions
+        // velocities and the mass-single temperature instead of four divisions
         const double irho = rcp_pos(rho);
         const double vx = u[RHOU] * irho, vy = u[RHOV] * irho, vz = u[RHOW] * irho;
         const double rhoe = u[RHOE] - (0.5 * rho) * ((vx * vx + vy * vy) + vz * vz);
@@ -423,13 +425,15 @@ __device__ __forceinline__ unsigned prims_cell(double* u, const double* spec) {
         u[VELY] = vy;
         u[VELZ] = vz;
         u[PRES] = p;
-        u[TEMP] = thermo_t<NS>(rho, p, spec);
+        // p / R / rho of the mass-single family as (p / rho) / R with the
+        // reciprocals above and from mfg_init (a few ulp from the two divisions)
+        u[TEMP] = (P.thermo_kind == MFG_THERMO_MASS_SINGLE) ? (p * irho) * P.inv_gas_R : thermo_t<NS>(rho, p, spec);
         wrote = (1u << DENS) | (1u << VELX) | (1u << VELY) | (1u << VELZ) | (1u << PRES) | (1u << TEMP);
-    } else if (P.conj_ht && vf == 0.0) {
+    } else if (P.conj_ht && is_zero_bits(vf)) {
         u[TEMP] = P.solid_temp;
         wrote = 1u << TEMP;
     }
-    if (P.do_ns && u[PRES] < 0.0) raise_status(MFG_STATUS_NEG_PRESSURE);
+    if (P.do_ns && is_negative(u[PRES])) raise_status(MFG_STATUS_NEG_PRESSURE);
     return wrote;
 }
 
@@ -530,7 +534,7 @@ __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, i
             for (int s = 0; s < NS; ++s) spec[s] = (s < ns) ? s1[s] : 0.0;
         } else {
 #pragma unroll
-            for (int s = 0; s < NS; ++s) spec[s] = add(spec[s], 0.0);
+            for (int s = 0; s < NS; ++s) spec[s] = plus_zero(spec[s]);
         }
     }
     const unsigned wrote = prims_cell<NS>(u, spec);
@@ -540,10 +544,10 @@ __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, i
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
         if (s >= ns) continue;
-        const double c0 = spec[s];
-        if (clip && spec[s] < 0.0) spec[s] = 0.0;
+        const bool neg = is_negative(spec[s]);
+        if (clip && neg) spec[s] = 0.0;
         // stored when the sub-step or the clipping may have changed it
-        if (chem || (clip && c0 < 0.0)) Sn(i, j, k, NFLO + s) = spec[s];
+        if (chem || (clip && neg)) Sn(i, j, k, NFLO + s) = spec[s];
     }
     if (!NORMS) return;
     // LinComb then Multiply, rounded as the reference (no contraction); acc
@@ -553,7 +557,7 @@ __device__ __forceinline__ void post_cell(const Fab& So, const Fab& Sn, int i, i
     for (int n = 0; n < NFLO; ++n) {
         const bool changed = n >= DENS && n <= TEMP;
         if (chem && !changed) {  // (a u + b u)^2 = 0 unless u is not finite
-            nonfinite |= !isfinite(u[n]);
+            nonfinite |= !is_finite_bits(u[n]);
             continue;
         }
         const double on = chem ? o6[changed ? n - DENS : 0] : So(i, j, k, n);
