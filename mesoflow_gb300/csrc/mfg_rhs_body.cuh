@@ -115,7 +115,11 @@ __device__ __forceinline__ double split_pres_m(double M, double alpha) {
 __device__ __forceinline__ void muscl(double uim2, double uL, double uR, double uip1, double& uLh, double& uRh) {
     double delt1 = uip1 - uR;
     double delt2 = uL - uim2;
-    double q = fabs((delt1 - delt2) * rcp_pos((fabs(delt1) + fabs(delt2)) + kTiny));
+    // max(|d1| + |d2|, 1e-20) for the reference's + 1e-20: the same ratio
+    // wherever the sum exceeds 1e-4 (the 1e-20 is below its rounding), a change
+    // below 1e-20 absolute in the limited state elsewhere, q = 0 for zero
+    // differences either way; the max runs on the integer pipe
+    double q = fabs((delt1 - delt2) * rcp_pos(max_nonneg(fabs(delt1) + fabs(delt2), kTiny)));
     double psi = 1.0 - q * q;
     double L = (0.5 * psi) * (delt1 + delt2);
     uLh = uL + 0.5 * L;
@@ -186,8 +190,8 @@ __device__ __forceinline__ bool face_active(const RhsBox& B, int d, int64_t t) {
     const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
     const int64_t oR = S.off(f.i, f.j, f.k);
     const double* vf = S.p + VFRAC * S.ns;
-    const double facevfrac = 0.5 * (vf[oR - sd] + vf[oR]);
-    return c_P.do_ns && nonneg_ge(facevfrac, 0.5);
+    // 0.5 (a + b) >= 0.5 exactly when a + b >= 1 (the halving is exact)
+    return c_P.do_ns && nonneg_ge(vf[oR - sd] + vf[oR], 1.0);
 }
 
 // SOLID_SIDE: the caller knows the face is not active (face_split_kernel);
@@ -212,14 +216,15 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
     bool fallback = false;
 #pragma unroll
     for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
-    const double facevfrac = 0.5 * (vf[oL] + vf[oR]);
-    const bool active = !SOLID_SIDE && P.do_ns && nonneg_ge(facevfrac, 0.5);
+    // face volume fraction 0.5 (a + b) >= 0.5, i.e. a + b >= 1 (the halving is exact)
+    const bool active = !SOLID_SIDE && P.do_ns && nonneg_ge(vf[oL] + vf[oR], 1.0);
 
     double fs[NFS];
 #pragma unroll
     for (int q = 0; q < NFS; ++q) fs[q] = 0.0;
     fs[FS_FLAGS] = __longlong_as_double((active ? 1 : 0) | ((P.do_ns && fallback) ? 2 : 0));  // bit pattern
     double uL[NCONS + NS], uR[NCONS + NS];  // AUSM+-up face states (orders 1, 2)
+    double vise = 0.0;                      // viscous work of the energy flux (orders 1, 2)
 
     if (active) {
         const int ord = P.order_hyp;
@@ -327,32 +332,39 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double* Vd = (d == 0) ? V0 : (d == 1) ? V1 : V2;
         const double* Vt1 = (t1 == 0) ? V0 : (t1 == 1) ? V1 : V2;
         const double* Vt2 = (t2 == 0) ? V0 : (t2 == 1) ? V1 : V2;
-        const double gn0 = (V0[oR] - V0[oL]) * ids, gn1 = (V1[oR] - V1[oL]) * ids, gn2 = (V2[oR] - V2[oL]) * ids;
+        // normal differences; the derivative (x 1/dx) is formed only where the
+        // divergence needs it, the shear terms fold the scale into an FMA
+        const double dn[3] = {V0[oR] - V0[oL], V1[oR] - V1[oL], V2[oR] - V2[oL]};
+        const double gnd = dn[d] * ids;
         const double d_t1 = ((Vd[oL + st1] + Vd[oR + st1]) - (Vd[oL - st1] + Vd[oR - st1])) * iq1;
         const double d_t2 = ((Vd[oL + st2] + Vd[oR + st2]) - (Vd[oL - st2] + Vd[oR - st2])) * iq2;
         const double t1_t1 = ((Vt1[oL + st1] + Vt1[oR + st1]) - (Vt1[oL - st1] + Vt1[oR - st1])) * iq1;
         const double t2_t2 = ((Vt2[oL + st2] + Vt2[oR + st2]) - (Vt2[oL - st2] + Vt2[oR - st2])) * iq2;
         // du/dx, dv/dy, dw/dz: the normal derivative along d, else the transverse one
-        const double dudx = (d == 0) ? gn0 : (t1 == 0) ? t1_t1 : t2_t2;
-        const double dvdy = (d == 1) ? gn1 : (t1 == 1) ? t1_t1 : t2_t2;
-        const double dwdz = (d == 2) ? gn2 : (t1 == 2) ? t1_t1 : t2_t2;
+        const double dudx = (d == 0) ? gnd : (t1 == 0) ? t1_t1 : t2_t2;
+        const double dvdy = (d == 1) ? gnd : (t1 == 1) ? t1_t1 : t2_t2;
+        const double dwdz = (d == 2) ? gnd : (t1 == 2) ? t1_t1 : t2_t2;
         // viscosity always from cells (i,j,k) and (i-1,j,k) (compute_flux_3d.H:179)
         const double mu = (P.visc_mode == MFG_TRANSPORT_CONST)
                               ? P.visc_hm
                               : harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR]),
                                               blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR - 1]));
         const double delu = (dudx + dvdy) + dwdz;
-        const double gn[3] = {gn0, gn1, gn2};
-        const double fvel[3] = {0.5 * (V0[oL] + V0[oR]), 0.5 * (V1[oL] + V1[oR]), 0.5 * (V2[oL] + V2[oR])};
+        // face velocities times 2 (the halving moves to the work sum)
+        const double fv2[3] = {V0[oL] + V0[oR], V1[oL] + V1[oR], V2[oL] + V2[oR]};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             // tau_{d a}: mu (2 dV_d/dx_d - 2/3 div V) on the diagonal, else
             // mu (dV_d/dx_a + dV_a/dx_d)
-            const double tn = (a == d) ? mu * (2.0 * gn[a] - kTwo3rd * delu)
-                                       : mu * (gn[a] + ((a == t1) ? d_t1 : d_t2));
+            const double tn = (a == d) ? mu * (2.0 * gnd - kTwo3rd * delu)
+                                       : mu * fma(dn[a], ids, (a == t1) ? d_t1 : d_t2);
             fs[FS_VIS + a] = tn;
-            fs[FS_VISE + a] = tn * fvel[a];
+            if (ord >= 4) fs[FS_VISE + a] = tn * (0.5 * fv2[a]);
         }
+        // orders 1, 2: the viscous work sum_a tau_{d a} v_a of the energy flux
+        // with fused multiply-adds (the face thread assembles that flux itself)
+        if (ord <= 2)
+            vise = 0.5 * fma(fs[FS_VIS + 0], fv2[0], fma(fs[FS_VIS + 1], fv2[1], fs[FS_VIS + 2] * fv2[2]));
     }
     if (P.do_ns) {
         // heat conduction (compute_flux_3d.H:373-374), conductivity from (i,j,k),(i-1,j,k)
@@ -391,11 +403,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
                 if (c == 1 + d) fh += fs[FS_PH];
                 F = (c < NCONS) ? fh : P.advect_flag[c - NCONS] * fh;
                 if (c >= RHOU && c <= RHOW) F -= fs[FS_VIS + c - 1];
-                if (c == RHOE) {
-                    F -= fs[FS_VISE + 0];
-                    F -= fs[FS_VISE + 1];
-                    F -= fs[FS_VISE + 2];
-                }
+                if (c == RHOE) F -= vise;
             }
             if (c == RHOE) F -= fs[FS_THERM];
             if (c >= NCONS) {
