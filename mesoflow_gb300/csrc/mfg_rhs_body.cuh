@@ -89,15 +89,16 @@ __device__ __forceinline__ void weno_face(const double s[6], double& up, double&
 // AUSM+-up split functions (flux_schemes.H:107-181), beta = 1/8.  The
 // supersonic branches of the pressure splits, (M + |M|)/(2M) and
 // (M - |M|)/(2M), are exactly 1 or 0 (with a zero's sign that no later
-// operation keeps), so they are selected instead of divided; the |M| <= 1
-// tests run on the integer pipe.
+// operation keeps), and those of the Mach splits, (M + |M|)/2 and
+// (M - |M|)/2, exactly M or +0 (2M and its halving are exact), so all four
+// are selects; the |M| <= 1 tests run on the integer pipe.
 __device__ __forceinline__ double split_mach_p(double M) {
     return abs_le(M, 1.0) ? (0.25 * (M + 1.0)) * (M + 1.0) + (0.125 * (M * M - 1.0)) * (M * M - 1.0)
-                          : 0.5 * (M + fabs(M));
+                          : (is_positive(M) ? M : 0.0);
 }
 __device__ __forceinline__ double split_mach_m(double M) {
     return abs_le(M, 1.0) ? (-0.25 * (M - 1.0)) * (M - 1.0) - (0.125 * (M * M - 1.0)) * (M * M - 1.0)
-                          : 0.5 * (M - fabs(M));
+                          : (is_negative(M) ? M : 0.0);
 }
 __device__ __forceinline__ double split_pres_p(double M, double alpha) {
     return abs_le(M, 1.0)
@@ -267,15 +268,15 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             }
             const double rL = uL[RHO], rR = uR[RHO];
             const double irL = rcp_pos(rL), irR = rcp_pos(rR);
-            const double vxL = uL[RHOU] * irL, vyL = uL[RHOV] * irL, vzL = uL[RHOW] * irL;
-            const double vxR = uR[RHOU] * irR, vyR = uR[RHOV] * irR, vzR = uR[RHOW] * irR;
-            const double kL = (vxL * vxL + vyL * vyL) + vzL * vzL;
-            const double kR = (vxR * vxR + vyR * vyR) + vzR * vzR;
-            const double pL = thermo_p<NS>(uL[RHOE] - (0.5 * rL) * kL, rL, uL + NCONS);
-            const double pR = thermo_p<NS>(uR[RHOE] - (0.5 * rR) * kR, rR, uR + NCONS);
+            // kinetic energy density |m|^2 / (2 rho) from the momenta and the
+            // normal velocity (the transverse velocities are not needed)
+            const double hkL = (0.5 * ((uL[RHOU] * uL[RHOU] + uL[RHOV] * uL[RHOV]) + uL[RHOW] * uL[RHOW])) * irL;
+            const double hkR = (0.5 * ((uR[RHOU] * uR[RHOU] + uR[RHOV] * uR[RHOV]) + uR[RHOW] * uR[RHOW])) * irR;
+            const double pL = thermo_p<NS>(uL[RHOE] - hkL, rL, uL + NCONS);
+            const double pR = thermo_p<NS>(uR[RHOE] - hkR, rR, uR + NCONS);
             const double gL = thermo_gamma<NS>(rL, uL + NCONS), gR = thermo_gamma<NS>(rR, uR + NCONS);
-            const double vL = (d == 0) ? vxL : (d == 1) ? vyL : vzL;
-            const double vR = (d == 0) ? vxR : (d == 1) ? vyR : vzR;
+            const double vL = ((d == 0) ? uL[RHOU] : (d == 1) ? uL[RHOV] : uL[RHOW]) * irL;
+            const double vR = ((d == 0) ? uR[RHOU] : (d == 1) ? uR[RHOV] : uR[RHOW]) * irR;
             const bool cg = P.thermo_kind == MFG_THERMO_MASS_SINGLE;
             // gamma/(gamma-1) and 2(gamma-1)/(gamma+1): constants of the single-gas
             // family, else per face state with reciprocals of the positive gamma +- 1
@@ -286,31 +287,44 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
                 afL = (2.0 * (gL - 1.0)) * rcp_pos(gL + 1.0);
                 afR = (2.0 * (gR - 1.0)) * rcp_pos(gR + 1.0);
             }
-            const double HL = gfL * (pL * irL) + 0.5 * kL;
-            const double HR = gfR * (pR * irR) + 0.5 * kR;
-            const double rho_half = 0.5 * (rL + rR);
-            // a_hat = a*^2 / max(a*, |v|): a* itself where a* >= |v| (subsonic
-            // side, a*^2/a* to within an ulp), one reciprocal otherwise
+            // total enthalpy gamma/(gamma-1) p/rho + |v|^2/2 = (gf p + |m|^2/(2 rho)) / rho
+            const double HL = fma(gfL, pL, hkL) * irL;
+            const double HR = fma(gfR, pR, hkR) * irR;
+            const double rsum = rL + rR;
+            // a_hat = a*^2 / max(a*, |v|) per side and its reciprocal: on the
+            // subsonic side (a* >= |v|) a* = a*^2 rsqrt(a*^2) and 1/a* = rsqrt(a*^2)
+            // (no square root and no reciprocal of the interface speed), else
+            // a*^2/|v| and |v|/a*^2
             double as2 = afL * HL;
-            double sq = sqrt(as2);
-            const double ahL = nonneg_ge(sq, fabs(vL)) ? sq : as2 * rcp_pos(fabs(vL));
+            double irs = rsqrt(as2);
+            double ahL = as2 * irs, iahL = irs;
+            if (!nonneg_ge(ahL, fabs(vL))) {
+                ahL = as2 * rcp_pos(fabs(vL));
+                iahL = fabs(vL) * rcp_pos(as2);
+            }
             as2 = afR * HR;
-            sq = sqrt(as2);
-            const double ahR = nonneg_ge(sq, fabs(vR)) ? sq : as2 * rcp_pos(fabs(vR));
-            const double ah = min_nonneg(ahL, ahR);
-            const double iah = rcp_pos(ah);
+            irs = rsqrt(as2);
+            double ahR = as2 * irs, iahR = irs;
+            if (!nonneg_ge(ahR, fabs(vR))) {
+                ahR = as2 * rcp_pos(fabs(vR));
+                iahR = fabs(vR) * rcp_pos(as2);
+            }
+            // a_1/2 = min(a_hat_L, a_hat_R) and its reciprocal from the same side
+            const bool left = nonneg_le(ahL, ahR);
+            const double ah = left ? ahL : ahR, iah = left ? iahL : iahR;
             const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
-            const double Mb2 = (0.5 * (vL * vL + vR * vR)) * (iah * iah);
+            const double Mb2 = 0.5 * (ML * ML + MR * MR);
             const double Mo = sqrt(min_nonneg(1.0, max_nonneg(Mb2, 0.3 * 0.3)));
             const double fa = Mo * (2.0 - Mo);
-            Mh = Mh - ((pos_part(1.0 - Mb2) * (pR - pL)) * (iah * iah)) * (0.25 * rcp_pos(fa * rho_half));
+            // pressure diffusion term (p_R - p_L) / (fa rho_1/2 a_1/2^2) / 4, rho_1/2 = (rho_L + rho_R) / 2
+            Mh = Mh - ((pos_part(1.0 - Mb2) * (pR - pL)) * (iah * iah)) * (0.5 * rcp_pos(fa * rsum));
             double modM = fabs(Mh);
             if (nonneg_le(modM, 0.3)) modM = (Mh * Mh + 0.3 * 0.3) * (1.0 / (2.0 * 0.3));
             const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
             const double PLp = split_pres_p(ML, alpha), PRm = split_pres_m(MR, alpha);
             double ph = PLp * pL + PRm * pR;
-            ph = ph - ((((0.75 * PLp) * PRm) * (rL + rR)) * (fa * ah)) * (vR - vL);
+            ph = ph - ((((0.75 * PLp) * PRm) * rsum) * (fa * ah)) * (vR - vL);
             fs[FS_LAMBDA] = ah;
             fs[FS_MH] = Mh;
             fs[FS_MODM] = modM;
