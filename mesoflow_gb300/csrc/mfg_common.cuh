@@ -183,4 +183,8 @@ __device__ __forceinline__ double rcp_pos(double x) {
     return fma(r, e, r);
 }
 
+// The same refinement for a finite, normal x of either sign (the hardware
+// approximation and the Newton steps are odd in x).
+__device__ __forceinline__ double rcp_nonzero(double x) { return rcp_pos(x); }
+
 }  // namespace mfg

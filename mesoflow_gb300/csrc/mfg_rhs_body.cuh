@@ -112,19 +112,23 @@ __device__ __forceinline__ double split_pres_m(double M, double alpha) {
 }
 
 // MUSCL state of component c with the Tatsumi-Martinelli-Jameson limiter
-// (compute_flux_3d.H:33-65): returns uL + L/2 and uR - L/2.
+// (compute_flux_3d.H:33-65): uL + L/2 and uR - L/2 with
+// L = psi (d1 + d2) / 2, psi = 1 - q^2, q = |d1 - d2| / (|d1| + |d2| + 1e-20),
+// d1 = u_{i+1} - u_R, d2 = u_L - u_{i-2}.  In closed form L/2 = d1 d2 / (d1 + d2)
+// when d1 and d2 have the same sign (then 1 - q^2 = 4 d1 d2 / (d1 + d2)^2) and
+// 0 otherwise (q = 1): the reference's expression equals this up to rounding
+// and terms of the order of its 1e-20 guard, and the closed form needs one
+// reciprocal and four fewer FP64 operations.  The same-sign test is on the
+// integer pipe (d1 d2 > 0).
 __device__ __forceinline__ void muscl(double uim2, double uL, double uR, double uip1, double& uLh, double& uRh) {
-    double delt1 = uip1 - uR;
-    double delt2 = uL - uim2;
-    // max(|d1| + |d2|, 1e-20) for the reference's + 1e-20: the same ratio
-    // wherever the sum exceeds 1e-4 (the 1e-20 is below its rounding), a change
-    // below 1e-20 absolute in the limited state elsewhere, q = 0 for zero
-    // differences either way; the max runs on the integer pipe
-    double q = fabs((delt1 - delt2) * rcp_pos(max_nonneg(fabs(delt1) + fabs(delt2), kTiny)));
-    double psi = 1.0 - q * q;
-    double L = (0.5 * psi) * (delt1 + delt2);
-    uLh = uL + 0.5 * L;
-    uRh = uR - 0.5 * L;
+    const double delt1 = uip1 - uR;
+    const double delt2 = uL - uim2;
+    const double p = delt1 * delt2;
+    const double s = delt1 + delt2;
+    // p > 0 implies s != 0; otherwise the reciprocal's value is not used
+    const double half = is_positive(p) ? p * rcp_nonzero(s) : 0.0;
+    uLh = uL + half;
+    uRh = uR - half;
 }
 
 // ---------------------------------------------------------------------------
@@ -315,13 +319,16 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
             const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
             const double Mb2 = 0.5 * (ML * ML + MR * MR);
-            const double Mo = sqrt(min_nonneg(1.0, max_nonneg(Mb2, 0.3 * 0.3)));
+            // M_o = sqrt(min(1, max(Mb^2, 0.3^2))) as x rsqrt(x) on the clamped x
+            const double xmo = min_nonneg(1.0, max_nonneg(Mb2, 0.3 * 0.3));
+            const double Mo = xmo * rsqrt(xmo);
             const double fa = Mo * (2.0 - Mo);
             // pressure diffusion term (p_R - p_L) / (fa rho_1/2 a_1/2^2) / 4, rho_1/2 = (rho_L + rho_R) / 2
             Mh = Mh - ((pos_part(1.0 - Mb2) * (pR - pL)) * (iah * iah)) * (0.5 * rcp_pos(fa * rsum));
             double modM = fabs(Mh);
             if (nonneg_le(modM, 0.3)) modM = (Mh * Mh + 0.3 * 0.3) * (1.0 / (2.0 * 0.3));
-            const double alpha = (3.0 * 0.0625) * (-4.0 + (5.0 * fa) * fa);
+            // alpha = 3/16 (-4 + 5 fa^2) as (15/16 fa) fa - 3/4
+            const double alpha = fma((15.0 / 16.0) * fa, fa, -0.75);
             const double PLp = split_pres_p(ML, alpha), PRm = split_pres_m(MR, alpha);
             double ph = PLp * pL + PRm * pR;
             ph = ph - ((((0.75 * PLp) * PRm) * rsum) * (fa * ah)) * (vR - vL);
