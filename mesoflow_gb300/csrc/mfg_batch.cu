@@ -274,9 +274,7 @@ __global__ void __launch_bounds__(BT) bk_fill_copy(const MBox* __restrict__ boxe
     if (ob < 0) continue;
     const MBox& o = boxes[ob];
     const Fab& S = src ? o.snew : o.sold;
-    const long long qs = S.off(cw[0], cw[1], cw[2]);
-    const long long qd = b.sb.off(i, j, k);
-    for (int c = 0; c < nc; ++c) b.sb.p[qd + c * b.sb.ns] = S.p[qs + c * S.ns];
+    copy_comps(b.sb.p + b.sb.off(i, j, k), b.sb.ns, S.p + S.off(cw[0], cw[1], cw[2]), S.ns, nc);
     TILE_END
 }
 
@@ -591,7 +589,7 @@ __global__ void __launch_bounds__(BT) bk_copy_old(const MBox* __restrict__ boxes
     const Valid v = valid_mbox(b);
     int i, j, k;
     cell_of(v, t, i, j, k);
-    for (int c = 0; c < nc; ++c) b.sold(i, j, k, c) = b.snew(i, j, k, c);
+    copy_comps(&b.sold(i, j, k, 0), b.sold.ns, &b.snew(i, j, k, 0), b.snew.ns, nc);
     TILE_END
 }
 

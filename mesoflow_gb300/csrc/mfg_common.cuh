@@ -183,6 +183,22 @@ __device__ __forceinline__ double rcp_pos(double x) {
     return fma(r, e, r);
 }
 
+// Copies nc components of one cell, src and dst component strides ss and ds,
+// four components' loads issued before their stores (the caller guarantees
+// the two do not overlap and src is not written meanwhile), so a thread keeps
+// four loads in flight instead of one.
+__device__ __forceinline__ void copy_comps(double* dst, int64_t ds, const double* src, int64_t ss, int nc) {
+    int c = 0;
+    for (; c + 4 <= nc; c += 4) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = __ldg(src + (c + u) * ss);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) dst[(c + u) * ds] = v[u];
+    }
+    for (; c < nc; ++c) dst[c * ds] = __ldg(src + c * ss);
+}
+
 // The same refinement for a finite, normal x of either sign (the hardware
 // approximation and the Newton steps are odd in x).
 __device__ __forceinline__ double rcp_nonzero(double x) { return rcp_pos(x); }

@@ -72,9 +72,8 @@ __global__ void copy_kernel(const FillBox* __restrict__ boxes, FillGeom G, const
     const int ob = owner[m0 + G.mlen[0] * (m1 + G.mlen[1] * m2)];
     if (ob < 0) return;  // not covered at this level
     const FillBox& o = boxes[ob];
-    const int64_t qs = o.src.off(w[0], w[1], w[2]);
-    const int64_t qd = b.sb.off(i, j, k);
-    for (int c = 0; c < ncomp; ++c) b.sb.p[qd + c * b.sb.ns] = o.src.p[qs + c * o.src.ns];
+    // Sborder is never a state FAB, and the states are not written here
+    copy_comps(b.sb.p + b.sb.off(i, j, k), b.sb.ns, o.src.p + o.src.off(w[0], w[1], w[2]), o.src.ns, ncomp);
 }
 
 // One launch per stage over the slabs of that stage only (blockIdx.y = slab).

@@ -359,18 +359,16 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double gnd = dn[d] * ids;
         const double d_t1 = ((Vd[oL + st1] + Vd[oR + st1]) - (Vd[oL - st1] + Vd[oR - st1])) * iq1;
         const double d_t2 = ((Vd[oL + st2] + Vd[oR + st2]) - (Vd[oL - st2] + Vd[oR - st2])) * iq2;
-        const double t1_t1 = ((Vt1[oL + st1] + Vt1[oR + st1]) - (Vt1[oL - st1] + Vt1[oR - st1])) * iq1;
-        const double t2_t2 = ((Vt2[oL + st2] + Vt2[oR + st2]) - (Vt2[oL - st2] + Vt2[oR - st2])) * iq2;
-        // du/dx, dv/dy, dw/dz: the normal derivative along d, else the transverse one
-        const double dudx = (d == 0) ? gnd : (t1 == 0) ? t1_t1 : t2_t2;
-        const double dvdy = (d == 1) ? gnd : (t1 == 1) ? t1_t1 : t2_t2;
-        const double dwdz = (d == 2) ? gnd : (t1 == 2) ? t1_t1 : t2_t2;
+        // the divergence's two transverse diagonal terms, each scaled inside
+        // the FMA that adds it: div V = dV_d/dx_d + dV_t1/dx_t1 + dV_t2/dx_t2
+        const double s1 = (Vt1[oL + st1] + Vt1[oR + st1]) - (Vt1[oL - st1] + Vt1[oR - st1]);
+        const double s2 = (Vt2[oL + st2] + Vt2[oR + st2]) - (Vt2[oL - st2] + Vt2[oR - st2]);
         // viscosity always from cells (i,j,k) and (i-1,j,k) (compute_flux_3d.H:179)
         const double mu = (P.visc_mode == MFG_TRANSPORT_CONST)
                               ? P.visc_hm
                               : harmonic_mean(blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR]),
                                               blend(P.visc_mode, P.visc_gas, P.visc_solid, vf[oR - 1]));
-        const double delu = (dudx + dvdy) + dwdz;
+        const double delu = fma(s2, iq2, fma(s1, iq1, gnd));
         // face velocities times 2 (the halving moves to the work sum)
         const double fv2[3] = {V0[oL] + V0[oR], V1[oL] + V1[oR], V2[oL] + V2[oR]};
 #pragma unroll
