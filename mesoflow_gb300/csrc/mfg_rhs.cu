@@ -66,9 +66,12 @@ __global__ void __launch_bounds__(TPB) face_split_kernel(RhsBox B) {
     const int d = blockIdx.y;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool act = false;
-    if (t < face_count(B, d)) {
-        act = face_active(B, d, t);
-        if (!act) face_body<NS, true>(B, d, t);
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    if (t < (int64_t)len[0] * len[1] * len[2]) {
+        const Idx3 f = delinear(t, lo, len);  // once for the test and the body
+        act = face_active(B, d, f);
+        if (!act) face_body_at<NS, true>(B, d, f);
     }
     const unsigned m = __ballot_sync(0xffffffffu, act);
     if (!m) return;
@@ -108,6 +111,7 @@ constexpr int64_t SWEEP_MIN_THREADS = 152 * 2 * SWEEP_TPB * 2;
 __global__ void __launch_bounds__(TPB) update_kernel(RhsBox B, int stage, double dt) {
     update_body(B, stage, dt, blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
+
 
 inline unsigned blocks_for(int64_t n) { return (unsigned)((n + TPB - 1) / TPB); }
 

@@ -184,13 +184,10 @@ __device__ __forceinline__ int64_t face_count(const RhsBox& B, int d) {
     return nf;
 }
 
-// Whether face t of direction d takes the flux branch of face_body
+// Whether face f of direction d takes the flux branch of face_body
 // (Navier-Stokes terms on and face volume fraction >= 1/2), by the same
 // arithmetic.
-__device__ __forceinline__ bool face_active(const RhsBox& B, int d, int64_t t) {
-    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
-    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
-    const Idx3 f = delinear(t, lo, len);
+__device__ __forceinline__ bool face_active(const RhsBox& B, int d, const Idx3& f) {
     const Fab& S = B.sb;
     const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
     const int64_t oR = S.off(f.i, f.j, f.k);
@@ -199,15 +196,13 @@ __device__ __forceinline__ bool face_active(const RhsBox& B, int d, int64_t t) {
     return c_P.do_ns && nonneg_ge(vf[oR - sd] + vf[oR], 1.0);
 }
 
-// SOLID_SIDE: the caller knows the face is not active (face_split_kernel);
-// the flux branch is compiled out and the remaining arithmetic is the same.
+// Face f of direction d.  SOLID_SIDE: the caller knows the face is not
+// active and the pass is the split form of orders 1/2 with Navier-Stokes
+// terms (face_split_kernel); the flux branch and the first-order fallback
+// test (used only by the flux branch and the stored face scalars of orders
+// 4/5) are compiled out, the remaining arithmetic is the same.
 template <int NS, bool SOLID_SIDE = false>
-__device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
-    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
-    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
-    const int64_t nf = (int64_t)len[0] * len[1] * len[2];
-    if (t >= nf) return;
-    const Idx3 f = delinear(t, lo, len);
+__device__ __forceinline__ void face_body_at(const RhsBox& B, int d, const Idx3& f) {
     const DevParams& P = c_P;
     const Fab& S = B.sb;
     const int64_t sd = (d == 0) ? 1 : (d == 1) ? S.js : S.ks;
@@ -219,8 +214,10 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
     const double* vf = S.p + VFRAC * S.ns;
 
     bool fallback = false;
+    if (!SOLID_SIDE) {
 #pragma unroll
-    for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
+        for (int q = -3; q <= 2; ++q) fallback |= below_one(vf[oR + q * sd]);
+    }
     // face volume fraction 0.5 (a + b) >= 0.5, i.e. a + b >= 1 (the halving is exact)
     const bool active = !SOLID_SIDE && P.do_ns && nonneg_ge(vf[oL] + vf[oR], 1.0);
 
@@ -394,7 +391,7 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
         const double* T = S.p + TEMP * S.ns;
         fs[FS_THERM] = kc * ((T[oR] - T[oL]) * B.idx[d]);
     }
-    if (P.do_ns && P.order_hyp <= 2) {
+    if (SOLID_SIDE || (P.do_ns && P.order_hyp <= 2)) {
         // AUSM+-up: the face thread holds the face states and the scheme scalars,
         // so it writes every component's complete flux (no per-component pass).
         const Fab& O = B.flx[d];
@@ -444,6 +441,16 @@ __device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
     const int64_t q = F.off(f.i, f.j, f.k);
 #pragma unroll
     for (int c = 0; c < NFS; ++c) F.p[q + c * F.ns] = fs[c];
+}
+
+// Face t (linear index over growHi(bx, d, 1)) of direction d.
+template <int NS>
+__device__ __forceinline__ void face_body(const RhsBox& B, int d, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1 + (e == d);
+    const int64_t nf = (int64_t)len[0] * len[1] * len[2];
+    if (t >= nf) return;
+    face_body_at<NS>(B, d, delinear(t, lo, len));
 }
 
 // ---------------------------------------------------------------------------
@@ -566,12 +573,10 @@ __device__ __forceinline__ void flux_body(const RhsBox& B, int d, int c, int64_t
 // ---------------------------------------------------------------------------
 // update_kernel: per (cell, component): divergence, masking, RK stage
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void update_body(const RhsBox& B, int stage, double dt, int n, int64_t t) {
-    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
-    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1;
-    const int64_t nc = (int64_t)len[0] * len[1] * len[2];
-    if (t >= nc) return;  // n: state component
-    const Idx3 x = delinear(t, lo, len);
+// One component n of the valid cell x (volume fraction vfrac): the body of
+// both launch shapes below, so they round identically.
+__device__ __forceinline__ void update_one(const RhsBox& B, int stage, double dt, int n, const Idx3& x,
+                                           double vfrac) {
     const DevParams& P = c_P;
     const bool advected = (n < NCONS) || (n >= NFLO);
     if (!advected && is_finite_bits(dt) && __double_as_longlong(dt) >= 0) {
@@ -606,7 +611,6 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
                       __fma_rn(Fy.p[oy] - Fy.p[oy + Fy.js], B.idx[1], mul(Fx.p[ox] - Fx.p[ox + 1], B.idx[0])));
         ds = plus_zero(ds);  // + source (compute_fluid_source is zero)
     }
-    const double vfrac = B.sb(x.i, x.j, x.k, VFRAC);
     const int nnull = (P.species_in_solid == 1) ? NFLO : NFLO + P.nspec;
     // vfrac tests and the NaN test on the integer pipe
     if (n != RHOE) {
@@ -634,6 +638,17 @@ __device__ __forceinline__ void update_body(const RhsBox& B, int stage, double d
         v = __fma_rn(2.0, v, B.sold(x.i, x.j, x.k, n));
         B.snew(x.i, x.j, x.k, n) = mul(v, kThird);
     }
+}
+
+__device__ __forceinline__ void update_body(const RhsBox& B, int stage, double dt, int n, int64_t t) {
+    int lo[3] = {B.lo[0], B.lo[1], B.lo[2]}, len[3];
+    for (int e = 0; e < 3; ++e) len[e] = B.hi[e] - B.lo[e] + 1;
+    const int64_t nc = (int64_t)len[0] * len[1] * len[2];
+    if (t >= nc) return;  // n: state component
+    const Idx3 x = delinear(t, lo, len);
+    const bool advected = (n < NCONS) || (n >= NFLO);
+    // the flux-less components' fast path reads no volume fraction
+    update_one(B, stage, dt, n, x, advected ? B.sb(x.i, x.j, x.k, VFRAC) : 0.0);
 }
 
 
