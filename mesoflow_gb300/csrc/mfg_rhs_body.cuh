@@ -292,27 +292,35 @@ __device__ __forceinline__ void face_body_at(const RhsBox& B, int d, const Idx3&
             const double HL = fma(gfL, pL, hkL) * irL;
             const double HR = fma(gfR, pR, hkR) * irR;
             const double rsum = rL + rR;
-            // a_hat = a*^2 / max(a*, |v|) per side and its reciprocal: on the
-            // subsonic side (a* >= |v|) a* = a*^2 rsqrt(a*^2) and 1/a* = rsqrt(a*^2)
-            // (no square root and no reciprocal of the interface speed), else
-            // a*^2/|v| and |v|/a*^2
-            double as2 = afL * HL;
-            double irs = rsqrt(as2);
-            double ahL = as2 * irs, iahL = irs;
-            if (!nonneg_ge(ahL, fabs(vL))) {
-                ahL = as2 * rcp_pos(fabs(vL));
-                iahL = fabs(vL) * rcp_pos(as2);
+            // a_hat = a*^2 / max(a*, |v|) per side, a_1/2 = min(a_hat_L, a_hat_R)
+            // and its reciprocal.  On a subsonic side (a* >= |v|, tested as
+            // a*^2 >= v^2) a_hat = a*, so when both sides are subsonic a_1/2 is
+            // the square root of the smaller a*^2: a_1/2 = m rsqrt(m) and
+            // 1/a_1/2 = rsqrt(m), one reciprocal square root and no reciprocal.
+            // Otherwise each side as a* or a*^2/|v| (and |v|/a*^2), the smaller.
+            const double as2L = afL * HL, as2R = afR * HR;
+            double ah, iah;
+            if (nonneg_ge(as2L, vL * vL) && nonneg_ge(as2R, vR * vR)) {
+                const double m = min_nonneg(as2L, as2R);
+                iah = rsqrt(m);
+                ah = m * iah;
+            } else {
+                double irs = rsqrt(as2L);
+                double ahL = as2L * irs, iahL = irs;
+                if (!nonneg_ge(ahL, fabs(vL))) {
+                    ahL = as2L * rcp_pos(fabs(vL));
+                    iahL = fabs(vL) * rcp_pos(as2L);
+                }
+                irs = rsqrt(as2R);
+                double ahR = as2R * irs, iahR = irs;
+                if (!nonneg_ge(ahR, fabs(vR))) {
+                    ahR = as2R * rcp_pos(fabs(vR));
+                    iahR = fabs(vR) * rcp_pos(as2R);
+                }
+                const bool left = nonneg_le(ahL, ahR);
+                ah = left ? ahL : ahR;
+                iah = left ? iahL : iahR;
             }
-            as2 = afR * HR;
-            irs = rsqrt(as2);
-            double ahR = as2 * irs, iahR = irs;
-            if (!nonneg_ge(ahR, fabs(vR))) {
-                ahR = as2 * rcp_pos(fabs(vR));
-                iahR = fabs(vR) * rcp_pos(as2);
-            }
-            // a_1/2 = min(a_hat_L, a_hat_R) and its reciprocal from the same side
-            const bool left = nonneg_le(ahL, ahR);
-            const double ah = left ? ahL : ahR, iah = left ? iahL : iahR;
             const double ML = vL * iah, MR = vR * iah;
             double Mh = split_mach_p(ML) + split_mach_m(MR);
             const double Mb2 = 0.5 * (ML * ML + MR * MR);
