@@ -83,12 +83,13 @@ __global__ void __launch_bounds__(TPB) face_split_kernel(RhsBox B) {
 }
 // The direction is the block's (blockIdx.y), uniform as in face_kernel, so
 // the compiler forms the same multiply-adds in both.
-// 128-thread blocks at 5 per SM (96 registers): 20 resident warps instead of
-// the 16 that 256-thread blocks at 116 registers give; the FP64-bound pass
-// issues 3% faster.
+// 128-thread blocks at 4 per SM (120 registers, no spills): after the FP64
+// operation cuts the body fits without spilling at 16 resident warps, which
+// measured 0.8% faster than 5 blocks at 96 registers with 80 bytes spilled
+// (and 6 blocks at 80 registers 1% slower).
 constexpr int LIST_TPB = 128;
 template <int NS>
-__global__ void __launch_bounds__(LIST_TPB, 5) face_list_kernel(RhsBox B) {
+__global__ void __launch_bounds__(LIST_TPB, 4) face_list_kernel(RhsBox B) {
     const int d = blockIdx.y;
     const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w < B.fcount[d]) face_body<NS>(B, d, B.flist[face_list_off(B, d) + w]);
