@@ -537,8 +537,20 @@ static int advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, d
     const size_t npart = (size_t)N * 1024;
     cudaStream_t cs = nullptr;
     cudaEvent_t ev = nullptr;
+    // every return after copies were queued on the copy stream first makes
+    // the caller's stream wait for them (the host views stay in use until then)
+    struct Join {
+        cudaStream_t cs = nullptr, st = nullptr;
+        cudaEvent_t ev = nullptr;
+        ~Join() {
+            if (cs && cudaEventRecord(ev, cs) == cudaSuccess) cudaStreamWaitEvent(st, ev, 0);
+        }
+    } join;
     if (h_state) {
         if (copy_stream(&cs, &ev) != cudaSuccess) return MFG_ERR_CUDA;
+        join.cs = cs;
+        join.st = st;
+        join.ev = ev;
         for (int b = 0; b < nbox; ++b)
             if (cudaMemcpyAsync(boxes[b].s_new.p, h_state[b].p, view_span_doubles(boxes[b].s_new) * sizeof(double),
                                 cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -580,8 +592,11 @@ static int advance_level(const mfg_box* boxes, int nbox, const mfg_geom* geom, d
             }
         }
     }
-    if (h_state && (cudaEventRecord(ev, cs) != cudaSuccess || cudaStreamWaitEvent(st, ev, 0) != cudaSuccess))
-        return MFG_ERR_CUDA;
+    if (h_state) {
+        join.cs = nullptr;  // joined here, with its errors reported
+        if (cudaEventRecord(ev, cs) != cudaSuccess || cudaStreamWaitEvent(st, ev, 0) != cudaSuccess)
+            return MFG_ERR_CUDA;
+    }
     std::vector<double> hn(resnorms ? N : 0);
     if (resnorms && cudaMemcpyAsync(hn.data(), acc, N * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return MFG_ERR_CUDA;
