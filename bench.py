@@ -248,8 +248,11 @@ def algorithmic(kind, case, a, nlaunch_per_step):
         # state components of the advected vector on the stencil extent, face scalars in, fluxes out
         return 8.0 * (Cadv * (B + 6) * B * B + 14 * faces + Cadv * faces)
     if kind == "face":
-        # conserved + species on the extent, velocities/T/vfrac around the face, face scalars out
-        return 8.0 * ((Cadv + 5) * (B + 6) * B * B + 14 * faces)
+        # conserved + species on the extent, velocities/T/vfrac around the face; out: the
+        # component fluxes (orders 1/2 with Navier-Stokes terms, AUSM+-up in the face pass)
+        # or the 14 face scalars the WENO flux pass reads
+        out = Cadv if (case.params.order_hyp <= 2 and case.params.do_ns) else 14
+        return 8.0 * ((Cadv + 5) * (B + 6) * B * B + out * faces)
     if kind == "update":
         # fluxes of 3 directions in, sborder/s_old/s_new in, s_new out
         return 8.0 * (3 * Cadv * faces + 4 * N * B ** 3)
